@@ -1,0 +1,180 @@
+/*
+ * slam_gb300 -- GB300-native dense RGB-D tracking (frame-to-model
+ * ICP + photometric odometry), C ABI.
+ *
+ * Drop-in for the reference class RGBDOdometryef
+ * (src/odom/RGBDOdometryef.h:28-131).  The reference takes GL textures
+ * (GPUTexture*, src/gl/types.h:9-37) and maps them through CUDA-GL interop;
+ * here every frame input is a plain DEVICE pointer with a row pitch in bytes,
+ * read on the handle's CUDA stream:
+ *   filtered depth   GL_LUMINANCE16UI  ->  const uint16_t*  (millimetres)
+ *   RGB              GL_RGBA8          ->  const uint8_t*   (RGBA, 4 B/px)
+ *   vertices/normals GL_RGBA32F        ->  const float*     (4 floats/px,
+ *                                           camera frame; z == 0 marks a hole)
+ * Poses are row-major: rot[9] = R (3x3), trans[3] = t, pose[16] = 4x4
+ * camera-to-world.
+ *
+ * Every function returns ODO_OK (0) or an error code and never exits the
+ * process (the reference's cudaSafeCall calls exit(0),
+ * src/cuda/convenience.cuh:64-71).  A handle owns its device buffers and one
+ * CUDA stream; it is not thread-safe, but separate handles are independent
+ * (no globals, unlike the reference's __constant__/texture globals,
+ * src/odom/utils.cu:548, 579-580).
+ *
+ * Call order per frame, as in the reference (src/apps/elastic_fusion_file.cpp:367-374):
+ *   odo_init_icp_model -> odo_init_rgb_model -> odo_init_icp_depth (or
+ *   odo_init_icp_maps) -> odo_init_rgb -> odo_get_incremental_transformation.
+ * NOTE (kept from the reference, src/odom/RGBDOdometryef.cpp:239,245): the
+ * depth pyramids used by the photometric term come from the vertex map last
+ * passed to odo_init_icp_model / odo_init_icp_maps, not from the depth image.
+ */
+#ifndef SLAM_GB300_H
+#define SLAM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ODO_OK 0
+#define ODO_ERR_ARG 1      /* bad argument (NULL, size, pitch, level) */
+#define ODO_ERR_CUDA 2     /* a CUDA runtime call failed; see odo_last_error */
+#define ODO_ERR_STATE 3    /* call-order violation */
+#define ODO_ERR_OOM 4      /* device allocation failed */
+#define ODO_ERR_TIMEOUT 5  /* a bounded device-side wait gave up */
+
+typedef struct odo_handle odo_t;
+
+/* The public metric members of RGBDOdometryef (src/odom/RGBDOdometryef.h:62-70). */
+typedef struct {
+    float lastICPError;
+    float lastICPCount;
+    float lastRGBError;
+    float lastRGBCount;
+    float lastSO3Error;
+    float lastSO3Count;
+    double lastA[36]; /* row-major 6x6 */
+    double lastb[6];
+} odo_stats;
+
+/* RGBDOdometryef::RGBDOdometryef, src/odom/RGBDOdometryef.cpp:21-111.
+ * Pass distThresh = 0.10f and angleThresh = sinf(20 deg) for the reference
+ * defaults (src/odom/RGBDOdometryef.h:35-36).  width/height must be >= 8 and
+ * <= 8192. */
+int odo_create(int width, int height, float cx, float cy, float fx, float fy, float distThresh, float angleThresh,
+               odo_t **out);
+int odo_destroy(odo_t *h);
+
+/* Use `stream` (a cudaStream_t) for all work of this handle; NULL restores
+ * the handle's own stream. */
+int odo_set_stream(odo_t *h, void *stream);
+
+/* initICP(GPUTexture* filteredDepth, depthCutoff), src/odom/RGBDOdometryef.cpp:118-142 */
+int odo_init_icp_depth(odo_t *h, const uint16_t *depth, size_t pitch_bytes, float depthCutoff);
+
+/* initICP(GPUTexture* verts, GPUTexture* norms, depthCutoff), src/odom/RGBDOdometryef.cpp:144-167 */
+int odo_init_icp_maps(odo_t *h, const float *verts, const float *norms, size_t pitch_bytes, float depthCutoff);
+
+/* initICPModel(verts, norms, depthCutoff, modelPose), src/odom/RGBDOdometryef.cpp:169-206 */
+int odo_init_icp_model(odo_t *h, const float *verts, const float *norms, size_t pitch_bytes, float depthCutoff,
+                       const float pose[16]);
+
+/* initRGB / initRGBModel / initFirstRGB, src/odom/RGBDOdometryef.cpp:237-265 */
+int odo_init_rgb(odo_t *h, const uint8_t *rgba, size_t pitch_bytes);
+int odo_init_rgb_model(odo_t *h, const uint8_t *rgba, size_t pitch_bytes);
+int odo_init_first_rgb(odo_t *h, const uint8_t *rgba, size_t pitch_bytes);
+
+/* getIncrementalTransformation, src/odom/RGBDOdometryef.cpp:267-595.
+ * trans/rot: in = previous pose, out = tracked pose.  Blocks until the
+ * result is on the host. */
+int odo_get_incremental_transformation(odo_t *h, float trans[3], float rot[9], int rgbOnly, float icpWeight,
+                                       int pyramid, int fastOdom, int so3);
+
+/* getCovariance, src/odom/RGBDOdometryef.cpp:597-600: inverse of lastA (row-major 6x6). */
+int odo_get_covariance(odo_t *h, double out[36]);
+
+/* lastICPError ... lastb of the last odo_get_incremental_transformation. */
+int odo_get_stats(odo_t *h, odo_stats *out);
+
+/* Iterations actually run by the last tracking call: out[0] = SO3
+ * iterations, out[1..3] = Gauss-Newton iterations at levels 0, 1, 2. */
+int odo_get_iterations(odo_t *h, int out[4]);
+
+/* Execution mode of odo_get_incremental_transformation:
+ *  ODO_MODE_GRAPH      (default) the whole tracking call is one captured CUDA
+ *                      graph: per iteration one association/reduction
+ *                      kernel and one photometric/solve kernel, the 6x6
+ *                      solve and pose update on the device;
+ *  ODO_MODE_STREAM     the same kernels launched one by one (no graph);
+ *  ODO_MODE_PERSISTENT one cooperative kernel per pyramid level that runs all
+ *                      iterations with grid-wide barriers. */
+#define ODO_MODE_GRAPH 0
+#define ODO_MODE_STREAM 1
+#define ODO_MODE_PERSISTENT 2
+int odo_set_mode(odo_t *h, int mode);
+
+/* Reduction precision:
+ *  ODO_PREC_FP32         FP32 accumulation as in the reference;
+ *  ODO_PREC_COMPENSATED  FP32 with Kahan-compensated per-thread sums and
+ *                        compensated tree reductions. */
+#define ODO_PREC_FP32 0
+#define ODO_PREC_COMPENSATED 1
+int odo_set_precision(odo_t *h, int precision);
+
+/* Bytes copied device -> host by one odo_get_incremental_transformation
+ * (the pose and statistics block). */
+size_t odo_state_bytes(void);
+
+/* Message of the last failing CUDA call on this handle ("" if none). */
+const char *odo_last_error(odo_t *h);
+const char *odo_status_string(int status);
+
+/* ---- parity / debugging access (used by the tests) ----
+ * Buffer ids: 0 depth pyramid (u16), 1 vmap_curr, 2 nmap_curr, 3 vmap_prev,
+ * 4 nmap_prev (planar float [3][rows][cols]), 5 lastDepth, 6 nextDepth
+ * (float), 7 lastImage, 8 nextImage, 9 lastNextImage (u8), 10 dIdx, 11 dIdy
+ * (int16), 12 correspondences (4 x int16 per pixel: u0, v0, diff, valid).
+ * Copies are dense (pitch = cols * element size) and synchronous. */
+int odo_debug_download(odo_t *h, int which, int level, void *host_dst, size_t bytes);
+int odo_debug_upload(odo_t *h, int which, int level, const void *host_src, size_t bytes);
+
+/* One ICP association/reduction pass at `level` with explicit poses
+ * (icpStep, src/odom/reduce.cu:418-490).  assoc (host, rows*cols int32,
+ * may be NULL) gets the gathered model pixel index or -1; out29 the 27
+ * products, residual^2 and inlier count (summed in FP64 from block
+ * partials). */
+int odo_debug_icp_step(odo_t *h, int level, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],
+                       const float tprev[3], int32_t *assoc, double out29[29]);
+
+/* One photometric residual pass (computeRgbResidual, src/odom/reduce.cu:869-935)
+ * writing buffer 12; out2 = {count, sum of squared differences (int32)}. */
+int odo_debug_rgb_residual(odo_t *h, int level, const float krkinv[9], const float kt[3], int32_t out2[2]);
+
+/* One photometric reduction (rgbStep, src/odom/reduce.cu:626-678) over
+ * buffer 12 at `level` with weight parameter sigma. */
+int odo_debug_rgb_step(odo_t *h, int level, float sigma, double out29[29]);
+
+/* One SO3 reduction at level 2 (so3Step, src/odom/reduce.cu:1082-1140) on
+ * lastNextImage vs nextImage. */
+int odo_debug_so3_step(odo_t *h, const float homography[9], const float kinv[9], const float krlr[9],
+                       double out11[11]);
+
+/* Derivative images of nextImage at all levels (computeDerivativeImages,
+ * src/odom/utils.cu:608-638). */
+int odo_debug_derivatives(odo_t *h);
+
+/* Times `reps` Gauss-Newton iterations at `level` (the two iteration kernels,
+ * launched back to back on the handle's stream with the pose state of the
+ * last tracking call) with CUDA events on that stream.  out_ms[0] / out_ms[1]
+ * = mean duration of the association/reduction kernel and of the
+ * photometric/solve kernel, each timed alone; out_ms[2] = mean time of one
+ * whole iteration.  Leaves the tracking state as it found it. */
+int odo_debug_time_iteration(odo_t *h, int level, int reps, float out_ms[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLAM_GB300_H */

@@ -1,0 +1,101 @@
+"""Loader for the native libraries built in-tree by slam_gb300/_build.py.
+
+There is no fallback: if libslam_gb300.so is missing or fails to load, every
+entry point raises.
+"""
+import ctypes
+import os
+
+from . import _build
+
+_LIB = None
+_SYNTH = None
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Returns the ctypes handle of libslam_gb300.so (declaring every C-ABI
+    function's signature)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise NativeError("libslam_gb300.so is not built (run __graft_entry__.build())")
+        _build.build()
+    L = ctypes.CDLL(_build.LIB)
+    _declare(L)
+    _LIB = L
+    return L
+
+
+def load_synth(build_if_missing=True):
+    global _SYNTH
+    if _SYNTH is not None:
+        return _SYNTH
+    if not os.path.exists(_build.SYNTH_LIB):
+        if not build_if_missing:
+            raise NativeError("libslam_synth.so is not built")
+        _build.build()
+    S = ctypes.CDLL(_build.SYNTH_LIB)
+    _SYNTH = S
+    return S
+
+
+c_int, c_float, c_double, c_void_p, c_size_t = ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t
+P = ctypes.POINTER
+
+
+class OdoStats(ctypes.Structure):
+    _fields_ = [("lastICPError", c_float), ("lastICPCount", c_float), ("lastRGBError", c_float),
+                ("lastRGBCount", c_float), ("lastSO3Error", c_float), ("lastSO3Count", c_float),
+                ("lastA", c_double * 36), ("lastb", c_double * 6)]
+
+
+# (name, restype, argtypes) of every function declared in include/slam_gb300.h
+SIGNATURES = [
+    ("odo_create", c_int, [c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_float, P(c_void_p)]),
+    ("odo_destroy", c_int, [c_void_p]),
+    ("odo_set_stream", c_int, [c_void_p, c_void_p]),
+    ("odo_init_icp_depth", c_int, [c_void_p, c_void_p, c_size_t, c_float]),
+    ("odo_init_icp_maps", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float]),
+    ("odo_init_icp_model", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float, P(c_float)]),
+    ("odo_init_rgb", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("odo_init_rgb_model", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("odo_init_first_rgb", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("odo_get_incremental_transformation", c_int,
+     [c_void_p, P(c_float), P(c_float), c_int, c_float, c_int, c_int, c_int]),
+    ("odo_get_covariance", c_int, [c_void_p, P(c_double)]),
+    ("odo_get_stats", c_int, [c_void_p, P(OdoStats)]),
+    ("odo_get_iterations", c_int, [c_void_p, P(c_int)]),
+    ("odo_set_mode", c_int, [c_void_p, c_int]),
+    ("odo_set_precision", c_int, [c_void_p, c_int]),
+    ("odo_state_bytes", c_size_t, []),
+    ("odo_last_error", ctypes.c_char_p, [c_void_p]),
+    ("odo_status_string", ctypes.c_char_p, [c_int]),
+    ("odo_debug_download", c_int, [c_void_p, c_int, c_int, c_void_p, c_size_t]),
+    ("odo_debug_upload", c_int, [c_void_p, c_int, c_int, c_void_p, c_size_t]),
+    ("odo_debug_icp_step", c_int, [c_void_p, c_int, P(c_float), P(c_float), P(c_float), P(c_float), c_void_p,
+                                   P(c_double)]),
+    ("odo_debug_rgb_residual", c_int, [c_void_p, c_int, P(c_float), P(c_float), P(ctypes.c_int32)]),
+    ("odo_debug_rgb_step", c_int, [c_void_p, c_int, c_float, P(c_double)]),
+    ("odo_debug_so3_step", c_int, [c_void_p, P(c_float), P(c_float), P(c_float), P(c_double)]),
+    ("odo_debug_derivatives", c_int, [c_void_p]),
+    ("odo_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
+]
+
+
+def _declare(L):
+    for name, res, args in SIGNATURES:
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args

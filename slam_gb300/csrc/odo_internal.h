@@ -1,0 +1,131 @@
+// Internal types shared by the host driver (odo_host.cpp) and the kernels
+// (odo_maps.cu, odo_track.cu).  Plain C++ (no CUDA headers beyond the
+// runtime's vector types), so g++ can compile the host side.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace slamgb {
+
+constexpr int kLevels = 3;
+
+// Pitched 2-D image view (pitch in bytes), like the reference's
+// PtrStepSz<T> (src/cuda/containers/kernel_containers.hpp:72-92).
+template <typename T>
+struct Img {
+    T *data;
+    size_t pitch;
+    int cols, rows;
+};
+
+// Planar 3-channel map [3][rows][cols] with a row pitch in bytes (the
+// reference's DeviceArray2D<float>(rows*3, cols), src/odom/RGBDOdometryef.cpp:97-101).
+struct Map3 {
+    float *data;
+    size_t pitch;
+    int cols, rows;
+};
+
+// Photometric correspondence, 8 bytes: model pixel (u0, v0), intensity
+// difference, valid flag.  Replaces the 16-byte DataTerm
+// (src/cuda/types.cuh:75-81); the live pixel is implied by the position.
+struct Corr {
+    int16_t u0, v0, diff, valid;
+};
+
+struct Intr {
+    float fx, fy, cx, cy;
+};
+
+// Device-resident state of one getIncrementalTransformation call.
+struct TrackState {
+    // inputs
+    float Rprev[9], tprev[3], Rprev_inv[9];
+    float icpWeight;
+    int rgbOnly, icp, rgb, so3;
+    // evolving pose
+    double resultRt[16];
+    double resultR[9];   // SO3 pre-alignment result
+    float Rcurr[9], tcurr[3];
+    float sigmaVal;
+    int level_break;     // rgbOnly early exit for the current level
+    // statistics (RGBDOdometryef public members)
+    float lastICPError, lastICPCount, lastRGBError, lastRGBCount, lastSO3Error, lastSO3Count;
+    double lastA[36], lastb[6];
+    int so3_iters, iters_run[kLevels];
+    int status;          // 0 ok, else ODO_ERR_* (timeouts of bounded waits)
+    // output
+    float out_R[9], out_t[3];
+};
+
+struct LevelArgs {
+    int level;
+    int cols, rows;
+    Intr K;
+    // ICP
+    Map3 vmap_curr, nmap_curr, vmap_prev, nmap_prev;
+    float distThres, angleThres;
+    // photometric
+    Img<const int16_t> dIdx, dIdy;
+    Img<const float> lastDepth, nextDepth;
+    Img<const uint8_t> lastImage, nextImage;
+    Img<Corr> corr;
+    float minScale;
+    float maxDepthDelta;
+    float sobelScale;
+};
+
+// Reduction workspace (owned by the handle).
+struct ReduceWs {
+    float *icp_part;       // [max_blocks][32]
+    float *rgb_part;       // [max_blocks][32]
+    int *res_part;         // [max_blocks][2]
+    unsigned *counters;    // [4]
+    int max_blocks;
+};
+
+// ---- launchers: preprocessing (odo_maps.cu) ----
+cudaError_t launch_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst, cudaStream_t s);
+cudaError_t launch_vmap_nmap(const Img<const uint16_t> *depth, const Map3 *vmap, const Map3 *nmap, const Intr *K,
+                             float cutoff, int nlevels, cudaStream_t s);
+cudaError_t launch_model_maps(const float *v4, const float *n4, size_t pitch4, int cols, int rows, const Map3 *vmap,
+                              const Map3 *nmap, int nlevels, int do_transform, const float R[9], const float t[3],
+                              float *vz, size_t vz_pitch, cudaStream_t s);
+cudaError_t launch_rgbd_level0(const float *vz, size_t vz_pitch, const uint8_t *rgba, size_t rgba_pitch, int cols,
+                               int rows, Img<float> depth0, Img<uint8_t> img0, int do_depth, cudaStream_t s);
+cudaError_t launch_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const uint8_t> isrc, Img<uint8_t> idst,
+                              int do_depth, cudaStream_t s);
+cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t> *dx, const Img<int16_t> *dy,
+                               int nlevels, cudaStream_t s);
+
+// ---- launchers: tracking (odo_track.cu) ----
+struct TrackLaunch {
+    int blocks_icp;    // grid of the association/reduction kernel
+    int blocks_rgb;    // grid of the photometric reduction kernel
+    int threads;       // block size of both
+    int precision;     // 0 FP32, 1 compensated
+};
+cudaError_t launch_track_begin(TrackState *st, cudaStream_t s);
+cudaError_t launch_so3(TrackState *st, Img<const uint8_t> last, Img<const uint8_t> next, Intr K2, cudaStream_t s);
+cudaError_t launch_level_iteration(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg, int iter,
+                                   cudaStream_t s);
+cudaError_t launch_level_persistent(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg,
+                                    int iterations, int sm_count, cudaStream_t s);
+cudaError_t launch_track_end(TrackState *st, cudaStream_t s);
+cudaError_t launch_iteration_part(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg, int iter,
+                                  int which, cudaStream_t s);
+int persistent_max_blocks(int threads);
+
+// debug single passes
+cudaError_t launch_debug_icp(const LevelArgs &L, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],
+                             const float tprev[3], int32_t *assoc, double *out29_dev, ReduceWs ws,
+                             const TrackLaunch &cfg, cudaStream_t s);
+cudaError_t launch_debug_rgb_residual(const LevelArgs &L, const float krkinv[9], const float kt[3], int *out2_dev,
+                                      ReduceWs ws, const TrackLaunch &cfg, cudaStream_t s);
+cudaError_t launch_debug_rgb_step(const LevelArgs &L, float sigma, double *out29_dev, ReduceWs ws,
+                                  const TrackLaunch &cfg, cudaStream_t s);
+cudaError_t launch_debug_so3(Img<const uint8_t> last, Img<const uint8_t> next, const float *params_dev,
+                             double *out11_dev, cudaStream_t s);
+
+}  // namespace slamgb
