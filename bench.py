@@ -275,8 +275,12 @@ def run_ours(args):
     fps_e2e = world * args.steps / (ms_e2e / 1000.0)
 
     # ---- roofline of the dominant kernel (association + residual pass) ----
+    odo.profile(reset=True)
     step(dframes[0])
+    phases = odo.profile(reset=True)
+    level_ms = {f"L{l}": odo.time_iteration(l, reps=50) for l in (2, 1)}
     k_ms, s_ms, it_ms = odo.time_iteration(0, reps=100)
+    level_ms["L0"] = [k_ms, s_ms, it_ms]
     n0 = cam.width * cam.height
     alg_bytes = BYTES_PER_PX_ITER * n0
     peak, peak_kind = measured_peaks()
@@ -287,6 +291,8 @@ def run_ours(args):
     if rank == 0:
         cpu = None
         try:
+            if args.cpu_seconds <= 0:
+                raise RuntimeError("skipped (--cpu-seconds 0)")
             from oracle import oracle
             oracle.set_threads(os.cpu_count() or 1)
             n, el = cpu_track(frames[:8], cam, seconds=args.cpu_seconds)
@@ -318,7 +324,8 @@ def run_ours(args):
                "frame_roofline_gbs": frame_bytes(cam, iters[1:]) / (ms / args.steps * 1e-3) / 1e9,
                "pose_error_vs_gt": {"rot_rad_mean": float(np.mean(rot)), "trans_m_mean": float(np.mean(tr)),
                                     "rot_rad_max": float(np.max(rot)), "trans_m_max": float(np.max(tr))},
-               "iterations": iters, "clocks": clk, "gpu_launches": launches_per_frame * args.steps,
+               "iterations": iters, "clocks": clk,
+               "iteration_ms_by_level": level_ms, "device_phases_us": phases, "gpu_launches": launches_per_frame * args.steps,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -173,6 +173,18 @@ int odo_debug_derivatives(odo_t *h);
  * whole iteration.  Leaves the tracking state as it found it. */
 int odo_debug_time_iteration(odo_t *h, int level, int reps, float out_ms[3]);
 
+/* Device-side phase timers accumulated over tracking calls (ns):
+ * out[0] last-block reduction of the block partials, out[1] FP64 solve and
+ * pose update, out[2] photometric residual finish, out[3] number of solves,
+ * out[4..7] parts of out[1]: LDLT, SE(3) exp + compose, FP32 pose + polar
+ * factor, next photometric warp.  reset != 0 clears them. */
+int odo_debug_profile(odo_t *h, double out[8], int reset);
+
+/* Per Gauss-Newton iteration of the last tracking call, 9 doubles per row:
+ * ICP inliers, photometric count, sigma, increment (v, omega).  Returns the
+ * number of rows written (<= max_rows); ODO_ERR_ARG on bad arguments. */
+int odo_debug_history(odo_t *h, double *out, int max_rows);
+
 #ifdef __cplusplus
 }
 #endif

@@ -405,15 +405,32 @@ void ORC(project_cloud)(const real *depth, int w, int h, real inv_fx, real inv_f
 /* ------------------------------------------------------------------ */
 /* Reductions                                                           */
 /* ------------------------------------------------------------------ */
-/* Per-row partial sums (sequential within a row), then rows summed in
- * order: deterministic for any thread count.  The reference's summation
+/* Per-pixel products are summed pairwise within each row, then the row sums
+ * pairwise: deterministic for any thread count.  The reference's summation
  * order (grid-stride + shuffle tree, src/odom/reduce.cu:90-255) depends on
  * its launch shape, so sums are compared to a tolerance. */
-static void accumulate_row7(real *acc, const real *row, real found) {
+static void products7(real *p, const real *row, real found) {
     int s = 0;
     for (int i = 0; i < 7; ++i)
-        for (int j = i; j < 7; ++j) acc[s++] += row[i] * row[j];
-    acc[28] += found;
+        for (int j = i; j < 7; ++j) p[s++] = row[i] * row[j];
+    p[28] = found;
+}
+
+/* Pairwise (cascade) sum of n records of ncomp values each (record stride
+ * `stride`), leaves of up to 8 records summed in order.  Deterministic and
+ * with O(log n) error growth, close to the GPU's tree reductions. */
+static void pairwise_sum(const real *v, int n, int stride, int ncomp, real *out) {
+    if (n <= 8) {
+        for (int k = 0; k < ncomp; ++k) out[k] = 0;
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < ncomp; ++k) out[k] += v[(size_t)i * stride + k];
+        return;
+    }
+    real a[32], b[32];
+    int m = n / 2;
+    pairwise_sum(v, m, stride, ncomp, a);
+    pairwise_sum(v + (size_t)m * stride, n - m, stride, ncomp, b);
+    for (int k = 0; k < ncomp; ++k) out[k] = a[k] + b[k];
 }
 
 /* ------------------------------------------------------------------ */
@@ -480,9 +497,11 @@ void ORC(icp_step)(const real Rcurr[9], const real tcurr[3], const real *vmap_cu
     a.distThres = distThres; a.angleThres = angleThres;
     a.cols = cols; a.rows = rows;
     real *part = (real *)calloc((size_t)rows * 29, sizeof(real));
-#pragma omp parallel for schedule(static)
+#pragma omp parallel
+    {
+    real *rb = (real *)malloc(sizeof(real) * (size_t)cols * 29);
+#pragma omp for schedule(static)
     for (int y = 0; y < rows; ++y) {
-        real *acc = part + (size_t)y * 29;
         for (int x = 0; x < cols; ++x) {
             v3 n, d, s;
             int idx, tf;
@@ -499,13 +518,14 @@ void ORC(icp_step)(const real Rcurr[9], const real tcurr[3], const real *vmap_cu
                 row[3] = c.x; row[4] = c.y; row[5] = c.z;
                 row[6] = dot(n_cp, sub(s_cp, d_cp));
             }
-            accumulate_row7(acc, row, (real)found);
+            products7(rb + (size_t)x * 29, row, (real)found);
         }
+        pairwise_sum(rb, cols, 29, 29, part + (size_t)y * 29);
+    }
+    free(rb);
     }
     real tot[29];
-    memset(tot, 0, sizeof(tot));
-    for (int y = 0; y < rows; ++y)
-        for (int k = 0; k < 29; ++k) tot[k] += part[(size_t)y * 29 + k];
+    pairwise_sum(part, rows, 29, 29, tot);
     for (int k = 0; k < 29; ++k) out29[k] = (double)tot[k];
     free(part);
 }
@@ -575,9 +595,11 @@ void ORC(rgb_step)(const orc_dataterm *corres, real sigma, const real *cloud, re
                    const int16_t *dIdx, const int16_t *dIdy, real sobelScale, int cols, int rows,
                    double out29[29]) {
     real *part = (real *)calloc((size_t)rows * 29, sizeof(real));
-#pragma omp parallel for schedule(static)
+#pragma omp parallel
+    {
+    real *rb = (real *)malloc(sizeof(real) * (size_t)cols * 29);
+#pragma omp for schedule(static)
     for (int y = 0; y < rows; ++y) {
-        real *acc = part + (size_t)y * 29;
         for (int x = 0; x < cols; ++x) {
             const orc_dataterm *c = &corres[(size_t)y * cols + x];
             real row[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -600,13 +622,14 @@ void ORC(rgb_step)(const orc_dataterm *corres, real sigma, const real *cloud, re
                 row[4] = pz * v0 - px * v2;
                 row[5] = -py * v0 + px * v1;
             }
-            accumulate_row7(acc, row, (real)(c->valid != 0));
+            products7(rb + (size_t)x * 29, row, (real)(c->valid != 0));
         }
+        pairwise_sum(rb, cols, 29, 29, part + (size_t)y * 29);
+    }
+    free(rb);
     }
     real tot[29];
-    memset(tot, 0, sizeof(tot));
-    for (int y = 0; y < rows; ++y)
-        for (int k = 0; k < 29; ++k) tot[k] += part[(size_t)y * 29 + k];
+    pairwise_sum(part, rows, 29, 29, tot);
     for (int k = 0; k < 29; ++k) out29[k] = (double)tot[k];
     free(part);
 }
@@ -633,10 +656,13 @@ void ORC(so3_step)(const uint8_t *lastImage, const uint8_t *nextImage, int cols,
         Hm.r[i] = mk(H[3 * i], H[3 * i + 1], H[3 * i + 2]);
         Ki.r[i] = mk(kinv[3 * i], kinv[3 * i + 1], kinv[3 * i + 2]);
     }
-#pragma omp parallel for schedule(static)
+#pragma omp parallel
+    {
+    real *rb = (real *)malloc(sizeof(real) * (size_t)cols * 11);
+#pragma omp for schedule(static)
     for (int y = 0; y < rows; ++y) {
-        real *acc = part + (size_t)y * 11;
         for (int x = 0; x < cols; ++x) {
+            real *acc = rb + (size_t)x * 11;
             v3 p = mk((real)x, (real)y, 1);
             v3 wp = mv(&Hm, p);
             int wx = f2i_rn(wp.x / wp.z), wy = f2i_rn(wp.y / wp.z);
@@ -662,14 +688,15 @@ void ORC(so3_step)(const uint8_t *lastImage, const uint8_t *nextImage, int cols,
             }
             int s = 0;
             for (int i = 0; i < 4; ++i)
-                for (int j = i; j < 4; ++j) acc[s++] += row[i] * row[j];
-            acc[10] += (real)found;
+                for (int j = i; j < 4; ++j) acc[s++] = row[i] * row[j];
+            acc[10] = (real)found;
         }
+        pairwise_sum(rb, cols, 11, 11, part + (size_t)y * 11);
+    }
+    free(rb);
     }
     real tot[11];
-    memset(tot, 0, sizeof(tot));
-    for (int y = 0; y < rows; ++y)
-        for (int k = 0; k < 11; ++k) tot[k] += part[(size_t)y * 11 + k];
+    pairwise_sum(part, rows, 11, 11, tot);
     for (int k = 0; k < 11; ++k) out11[k] = (double)tot[k];
     free(part);
 }
@@ -807,7 +834,7 @@ static void rodrigues(const double *src, double *R) {
 static void polar33(const real *Min, real *Rout) {
     double X[9];
     for (int k = 0; k < 9; ++k) X[k] = (double)Min[k];
-    for (int it = 0; it < 4; ++it) {
+    for (int it = 0; it < 2; ++it) {
         double Xi[9];
         inv33_d(X, Xi);
         for (int i = 0; i < 3; ++i)
@@ -864,6 +891,8 @@ typedef struct {
     orc_stats st;
     double lastA[36], lastb[6];
     int so3_iters, iters_run[NUM_PYRS];
+    int nhist;
+    double hist[32][9];
 } orc_odo;
 
 /* CameraModel::operator()(level), src/sensors/Camera.h:14-18 */
@@ -1074,6 +1103,7 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
     }
 
     int iterations[3] = {fastOdom ? 3 : 10, pyramid ? 5 : 0, pyramid ? 4 : 0};
+    o->nhist = 0;
     real Rprev_inv[9];
     inv33_r(Rprev, Rprev_inv);
     double resultRt[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -1150,6 +1180,13 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
             }
             double result[6];
             ldlt_solve_d(6, o->lastA, o->lastb, result);
+            if (o->nhist < 32) {
+                double *hr = o->hist[o->nhist++];
+                hr[0] = icp29[28];
+                hr[1] = o->st.lastRGBCount;
+                hr[2] = sigmaVal;
+                for (int k = 0; k < 6; ++k) hr[3 + k] = result[k];
+            }
 
             /* computeUpdateSE3, src/odom/utils.h:54-74 */
             double Rinc[9];
@@ -1186,7 +1223,7 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
     }
     if (rgb) {
         real dx = tcurr[0] - tprev[0], dy = tcurr[1] - tprev[1], dz = tcurr[2] - tprev[2];
-        if (SQRT(dx * dx + dy * dy + dz * dz) > (real)0.3) {
+        if ((double)SQRT(dx * dx + dy * dy + dz * dz) > 0.3) {
             memcpy(Rcurr, Rprev, sizeof(Rcurr));
             memcpy(tcurr, tprev, sizeof(tcurr));
         }
@@ -1232,5 +1269,10 @@ void *ORC(odo_buffer)(orc_odo *o, int which, int level) {
     return NULL;
 }
 int ORC(real_size)(void) { return (int)sizeof(real); }
+int ORC(odo_history)(orc_odo *o, double *out, int max_rows) {
+    int n = o->nhist < max_rows ? o->nhist : max_rows;
+    memcpy(out, o->hist, sizeof(double) * 9 * (size_t)n);
+    return n;
+}
 
 #endif /* ORC_REAL_F32 || ORC_REAL_F64 */

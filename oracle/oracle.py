@@ -308,6 +308,11 @@ class Odometry:
         self.k.f("odo_iters")(self._h, out)
         return list(out)
 
+    def history(self):
+        out = np.zeros((32, 9), np.float64)
+        n = self.k.f("odo_history")(self._h, _p(out), 32)
+        return out[:n]
+
     @property
     def stats(self):
         s = self._stats

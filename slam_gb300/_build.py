@@ -64,7 +64,8 @@ def build(force=False, verbose=False, extra_nvcc=()):
         objs.append(obj)
         if force or _newer(obj, [path, __file__] + headers):
             if src.endswith(".cu"):
-                cmd = [NVCC, *ARCH, *COMMON, *NUMERIC, *extra_nvcc, "-c", path, "-o", obj]
+                cmd = [NVCC, *ARCH, *COMMON, *NUMERIC, "-Xcompiler", "-ffp-contract=off", *extra_nvcc, "-c", path,
+                       "-o", obj]
             else:
                 cmd = [NVCC, *COMMON, "-Xcompiler", "-ffp-contract=off", "-c", path, "-o", obj]
             jobs.append(cmd)

@@ -77,6 +77,7 @@ struct odo_handle {
     DImg<uint8_t> lastImage[kLevels], imgA[kLevels], imgB[kLevels];
     DImg<int16_t> dIdx[kLevels], dIdy[kLevels];
     DImg<Corr> corr[kLevels];
+    DImg<uint8_t> cand[kLevels];
     DImg<float> vz;
     ReduceWs ws{};
     TrackState *st_dev = nullptr;
@@ -137,6 +138,32 @@ cudaError_t alloc_map(odo_t *h, DMap &m, int cols, int rows) {
     return e;
 }
 
+// pow(minimumGradientMagnitudes[l], 2) / pow(sobelScale, 2) with the
+// magnitudes 5/3/1 and sobelScale 1/8 (src/odom/RGBDOdometryef.cpp:34-35,
+// 108-110, 439).
+float min_scale(int l) {
+    const float minGrad[kLevels] = {5, 3, 1};
+    const float sobelScale = (float)(1.0 / pow(2.0, 3));
+    return (float)(pow(minGrad[l], 2.0) / pow((double)sobelScale, 2.0));
+}
+
+cudaError_t enqueue_derivatives(odo_t *h, cudaStream_t s) {
+    Img<const uint8_t> src[kLevels];
+    Img<int16_t> dx[kLevels], dy[kLevels];
+    Img<const float> nd[kLevels];
+    Img<uint8_t> cand[kLevels];
+    float ms[kLevels];
+    for (int l = 0; l < kLevels; ++l) {
+        src[l] = h->nextImage()[l].cimg();
+        dx[l] = h->dIdx[l].img();
+        dy[l] = h->dIdy[l].img();
+        nd[l] = h->nextDepth[l].cimg();
+        cand[l] = h->cand[l].img();
+        ms[l] = min_scale(l);
+    }
+    return launch_derivatives(src, dx, dy, nd, cand, ms, kLevels, s);
+}
+
 LevelArgs level_args(odo_t *h, int l) {
     LevelArgs L;
     L.level = l;
@@ -156,11 +183,9 @@ LevelArgs level_args(odo_t *h, int l) {
     L.lastImage = h->lastImage[l].cimg();
     L.nextImage = h->nextImage()[l].cimg();
     L.corr = h->corr[l].img();
-    // minimumGradientMagnitudes 5/3/1 and sobelScale 1/8
-    // (src/odom/RGBDOdometryef.cpp:34-35, 108-110, 439)
-    const float minGrad[kLevels] = {5, 3, 1};
+    L.cand = h->cand[l].cimg();
     const float sobelScale = (float)(1.0 / pow(2.0, 3));
-    L.minScale = (float)(pow(minGrad[l], 2.0) / pow((double)sobelScale, 2.0));
+    L.minScale = min_scale(l);
     L.maxDepthDelta = 0.07f;  // maxDepthDeltaRGB, src/odom/RGBDOdometryef.cpp:36
     L.sobelScale = sobelScale;
     return L;
@@ -191,16 +216,7 @@ cudaError_t enqueue_track(odo_t *h, const int iterations[kLevels], int icp, int 
     cudaStream_t s = h->stream;
     cudaError_t e = cudaMemcpyAsync(h->st_dev, h->st_host, sizeof(TrackState), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
-    if (rgb) {
-        Img<const uint8_t> src[kLevels];
-        Img<int16_t> dx[kLevels], dy[kLevels];
-        for (int l = 0; l < kLevels; ++l) {
-            src[l] = h->nextImage()[l].cimg();
-            dx[l] = h->dIdx[l].img();
-            dy[l] = h->dIdy[l].img();
-        }
-        if ((e = launch_derivatives(src, dx, dy, kLevels, s)) != cudaSuccess) return e;
-    }
+    if (rgb && (e = enqueue_derivatives(h, s)) != cudaSuccess) return e;
     if (so3) {
         const int L2 = 2;
         if ((e = launch_so3(h->st_dev, h->lastNextImage()[L2].cimg(), h->nextImage()[L2].cimg(), h->intr(L2), s)) !=
@@ -307,7 +323,8 @@ int odo_create(int width, int height, float cx, float cy, float fx, float fy, fl
             (e = alloc_img(h, h->imgB[l], w, hh)) != cudaSuccess ||
             (e = alloc_img(h, h->dIdx[l], w, hh)) != cudaSuccess ||
             (e = alloc_img(h, h->dIdy[l], w, hh)) != cudaSuccess ||
-            (e = alloc_img(h, h->corr[l], w, hh)) != cudaSuccess)
+            (e = alloc_img(h, h->corr[l], w, hh)) != cudaSuccess ||
+            (e = alloc_img(h, h->cand[l], w, hh)) != cudaSuccess)
             return bail(e, "device allocation");
     }
     if ((e = alloc_img(h, h->vz, width, height)) != cudaSuccess) return bail(e, "device allocation");
@@ -612,15 +629,24 @@ int odo_debug_so3_step(odo_t *h, const float homography[9], const float kinv[9],
 
 int odo_debug_derivatives(odo_t *h) {
     if (!h) return ODO_ERR_ARG;
-    Img<const uint8_t> src[kLevels];
-    Img<int16_t> dx[kLevels], dy[kLevels];
-    for (int l = 0; l < kLevels; ++l) {
-        src[l] = h->nextImage()[l].cimg();
-        dx[l] = h->dIdx[l].img();
-        dy[l] = h->dIdy[l].img();
-    }
-    CK(launch_derivatives(src, dx, dy, kLevels, h->stream));
+    CK(enqueue_derivatives(h, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    return ODO_OK;
+}
+
+int odo_debug_history(odo_t *h, double *out, int max_rows) {
+    if (!h || !out || max_rows < 0) return ODO_ERR_ARG;
+    int n = h->st_host->nhist < max_rows ? h->st_host->nhist : max_rows;
+    for (int r = 0; r < n; ++r)
+        for (int k = 0; k < 9; ++k) out[r * 9 + k] = h->st_host->hist[r][k];
+    return n;
+}
+
+int odo_debug_profile(odo_t *h, double out[8], int reset) {
+    if (!h || !out) return ODO_ERR_ARG;
+    for (int k = 0; k < 8; ++k) out[k] = h->st_host->prof[k];
+    if (reset)
+        for (int k = 0; k < 8; ++k) h->st_host->prof[k] = 0;
     return ODO_OK;
 }
 

@@ -48,6 +48,7 @@ struct TrackState {
     double resultRt[16];
     double resultR[9];   // SO3 pre-alignment result
     float Rcurr[9], tcurr[3];
+    float krkinv[9], kt[3];  // photometric warp of the next iteration (same level)
     float sigmaVal;
     int level_break;     // rgbOnly early exit for the current level
     // statistics (RGBDOdometryef public members)
@@ -55,6 +56,15 @@ struct TrackState {
     double lastA[36], lastb[6];
     int so3_iters, iters_run[kLevels];
     int status;          // 0 ok, else ODO_ERR_* (timeouts of bounded waits)
+    // device-side phase timers (ns, accumulated; globaltimer): [0] last-block
+    // partial reduction, [1] FP64 solve + pose update, [2] residual finish,
+    // [3] number of solves, [4] LDLT, [5] exp + compose, [6] FP32 pose +
+    // polar factor, [7] next warp
+    double prof[8];
+    // per Gauss-Newton iteration (debugging): icp count, rgb count, sigma,
+    // increment x[0..5]
+    int nhist;
+    double hist[32][9];
     // output
     float out_R[9], out_t[3];
 };
@@ -71,6 +81,7 @@ struct LevelArgs {
     Img<const float> lastDepth, nextDepth;
     Img<const uint8_t> lastImage, nextImage;
     Img<Corr> corr;
+    Img<const uint8_t> cand;  // pose-independent photometric preconditions, per pixel
     float minScale;
     float maxDepthDelta;
     float sobelScale;
@@ -97,6 +108,7 @@ cudaError_t launch_rgbd_level0(const float *vz, size_t vz_pitch, const uint8_t *
 cudaError_t launch_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const uint8_t> isrc, Img<uint8_t> idst,
                               int do_depth, cudaStream_t s);
 cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t> *dx, const Img<int16_t> *dy,
+                               const Img<const float> *nextDepth, const Img<uint8_t> *cand, const float *minScale,
                                int nlevels, cudaStream_t s);
 
 // ---- launchers: tracking (odo_track.cu) ----

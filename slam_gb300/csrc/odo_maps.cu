@@ -254,9 +254,17 @@ __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.000
 struct DerivArgs {
     Img<const uint8_t> src[kLevels];
     Img<int16_t> dx[kLevels], dy[kLevels];
+    Img<const float> depth[kLevels];
+    Img<uint8_t> cand[kLevels];
+    float minScale[kLevels];
 };
 
-// applyKernel (src/odom/utils.cu:582-606), all levels in one launch.
+// applyKernel (src/odom/utils.cu:582-606), all levels in one launch.  Also
+// evaluates, once per frame, the pose-independent preconditions of a
+// photometric correspondence (RGBResidual::getProducts,
+// src/odom/reduce.cu:782-810: j0 < cols-5, i < rows-1, no zero intensity in
+// the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
+// into a byte mask, so the per-iteration pass reads one byte per pixel.
 __global__ void k_derivatives(DerivArgs a) {
     const int l = blockIdx.z;
     const Img<const uint8_t> src = a.src[l];
@@ -273,8 +281,23 @@ __global__ void k_derivatives(DerivArgs a) {
             --kernelIndex;
         }
     }
-    at(a.dx[l], x, y) = dxVal;
-    at(a.dy[l], x, y) = dyVal;
+    const short sx = dxVal, sy = dyVal;
+    at(a.dx[l], x, y) = sx;
+    at(a.dy[l], x, y) = sy;
+    const int cols = src.cols, rows = src.rows, i = y, j0 = x;
+    bool c = false;
+    if (j0 < cols - 5 && i < rows - 1) {
+        bool valid = true;
+        for (int u = max(i - 2, 0); u < min(i + 2, rows); u++) {
+            const uint8_t *r = rowp(src.data, src.pitch, u);
+            for (int v = max(j0 - 2, 0); v < min(j0 + 2, cols); v++) valid = valid && (r[v] > 0);
+        }
+        if (valid) {
+            float mTwo = (sx * sx) + (sy * sy);
+            c = mTwo >= a.minScale[l] && !isnan(at(a.depth[l], x, y));
+        }
+    }
+    at(a.cand[l], x, y) = c ? 1 : 0;
 }
 
 inline dim3 grid2(int cols, int rows, int z = 1) { return dim3((cols + BX - 1) / BX, (rows + BY - 1) / BY, z); }
@@ -338,12 +361,16 @@ cudaError_t launch_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const 
 }
 
 cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t> *dx, const Img<int16_t> *dy,
+                               const Img<const float> *nextDepth, const Img<uint8_t> *cand, const float *minScale,
                                int nlevels, cudaStream_t s) {
     DerivArgs a;
     for (int l = 0; l < nlevels; ++l) {
         a.src[l] = src[l];
         a.dx[l] = dx[l];
         a.dy[l] = dy[l];
+        a.depth[l] = nextDepth[l];
+        a.cand[l] = cand[l];
+        a.minScale[l] = minScale[l];
     }
     k_derivatives<<<grid2(src[0].cols, src[0].rows, nlevels), dim3(BX, BY), 0, s>>>(a);
     return cudaGetLastError();

@@ -114,7 +114,7 @@ SE3_HD void rodrigues(const double *src, double *R) {
 SE3_HD void polar33(const float *Min, float *Rout) {
     double X[9];
     for (int k = 0; k < 9; ++k) X[k] = (double)Min[k];
-    for (int it = 0; it < 4; ++it) {
+    for (int it = 0; it < 2; ++it) {
         double Xi[9];
         inv33(X, Xi);
         double Y[9];
@@ -129,10 +129,20 @@ SE3_HD void polar33(const float *Min, float *Rout) {
 // computeUpdateSE3, src/odom/utils.h:54-74): solve A x = b, left-compose
 // [R(x[3:6]) | x[0:3]] onto resultRt (FP64 4x4 row-major), then
 // currentT = [Rprev | tprev] * rgbOdom^-1 in FP32.
+#if defined(__CUDA_ARCH__)
+#define SE3_MARK(i) \
+    if (marks) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(marks[i]))
+#else
+#define SE3_MARK(i)
+#endif
 SE3_HD void gn_update(const double *A, const double *b, double *resultRt, const float *Rprev, const float *tprev,
-                      float *Rcurr, float *tcurr) {
+                      float *Rcurr, float *tcurr, double *x_out = nullptr, unsigned long long *marks = nullptr) {
     double x[6];
+    SE3_MARK(0);
     ldlt_solve<double, 6>(A, b, x);
+    SE3_MARK(1);
+    if (x_out)
+        for (int k = 0; k < 6; ++k) x_out[k] = x[k];
     double Rinc[9];
     rodrigues(x + 3, Rinc);
     const double Rt4[16] = {Rinc[0], Rinc[1], Rinc[2], x[0], Rinc[3], Rinc[4], Rinc[5], x[1],
@@ -145,6 +155,7 @@ SE3_HD void gn_update(const double *A, const double *b, double *resultRt, const 
             nr[a * 4 + c] = s;
         }
     for (int k = 0; k < 16; ++k) resultRt[k] = nr[k];
+    SE3_MARK(2);
     float oR[9], ot[3];
     for (int a = 0; a < 3; ++a) {
         for (int c = 0; c < 3; ++c) oR[a * 3 + c] = (float)resultRt[a * 4 + c];
@@ -159,6 +170,7 @@ SE3_HD void gn_update(const double *A, const double *b, double *resultRt, const 
     for (int a = 0; a < 3; ++a)
         tcurr[a] = (Rprev[a * 3] * it[0] + Rprev[a * 3 + 1] * it[1] + Rprev[a * 3 + 2] * it[2]) + tprev[a];
     polar33(cR, Rcurr);
+    SE3_MARK(3);
 }
 
 // K R K^-1 and K t of resultRt^-1 for the photometric warp

@@ -228,5 +228,24 @@ class RGBDOdometry:
         self._check(self._L.odo_debug_time_iteration(self._h, level, int(reps), out), "time_iteration")
         return list(out)
 
+    def profile(self, reset=True):
+        """Device phase timers in microseconds per solve: (partial reduction,
+        FP64 solve + pose update, residual finish, number of solves)."""
+        out = np.zeros(8, np.float64)
+        self._check(self._L.odo_debug_profile(self._h, _dptr(out), int(bool(reset))), "profile")
+        n = max(out[3], 1.0)
+        us = lambda k: out[k] / n / 1e3
+        return {"reduce_us": us(0), "solve_us": us(1), "residual_finish_us": us(2), "solves": int(out[3]),
+                "ldlt_us": us(4), "exp_compose_us": us(5), "pose_polar_us": us(6), "warp_us": us(7)}
+
+    def history(self):
+        """[n, 9] per-iteration record of the last tracking call: ICP inliers,
+        photometric count, sigma, increment (v, omega)."""
+        out = np.zeros((32, 9), np.float64)
+        n = self._L.odo_debug_history(self._h, _dptr(out), 32)
+        if n < 0:
+            self._check(n, "history")
+        return out[:n]
+
     def debug_derivatives(self):
         self._check(self._L.odo_debug_derivatives(self._h), "debug_derivatives")

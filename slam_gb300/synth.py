@@ -94,13 +94,15 @@ def rotvec_to_R(w):
 
 
 def R_to_rotvec(R):
+    """Rotation vector of R; atan2 form, accurate for tiny angles."""
     R = np.asarray(R, dtype=np.float64)
-    c = max(-1.0, min(1.0, (np.trace(R) - 1) / 2))
-    th = math.acos(c)
-    if th < 1e-12:
+    w = 0.5 * np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]])
+    s = np.linalg.norm(w)
+    c = (np.trace(R) - 1) / 2
+    th = math.atan2(s, c)
+    if s < 1e-300:
         return np.zeros(3)
-    w = np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]) / (2 * math.sin(th))
-    return w * th
+    return w / s * th
 
 
 def pose(R, t):
