@@ -44,6 +44,7 @@ extern "C" {
 #define ODO_ERR_STATE 3    /* call-order violation */
 #define ODO_ERR_OOM 4      /* device allocation failed */
 #define ODO_ERR_TIMEOUT 5  /* a bounded device-side wait gave up */
+#define ODO_ERR_SIZE 6     /* image larger than the allocation-free entry point's fixed scratch allows */
 
 typedef struct odo_handle odo_t;
 
@@ -184,6 +185,39 @@ int odo_debug_profile(odo_t *h, double out[8], int reset);
  * ICP inliers, photometric count, sigma, increment (v, omega).  Returns the
  * number of rows written (<= max_rows); ODO_ERR_ARG on bad arguments. */
 int odo_debug_history(odo_t *h, double *out, int max_rows);
+
+/* ---- allocation-free ICP reduction ----
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory after start-up -- a tracker running inside
+ * a fixed device-memory budget, or a real-time loop where cudaMalloc/cudaFree
+ * would synchronise the device and stall other streams.  It computes one
+ * ICP association + reduction pass like the reference's icpStep
+ * (src/odom/reduce.cu:418-490): the caller passes the four planar maps
+ * ([3][rows][cols] float, row pitch in bytes) and the poses; it returns the
+ * 6x6 matrix A (row-major), b and {sum of squared residuals, inliers} on the
+ * host, as icpStep does.  It needs no handle and allocates nothing: its
+ * block partials live in one fixed device array of this library
+ * (ODO_NOALLOC_SCRATCH_BYTES, held by every device that loads the library
+ * until the process exits).
+ *  - Images up to ODO_NOALLOC_MAX_PIXELS pixels (cols * rows); larger ones
+ *    return ODO_ERR_SIZE without touching the GPU.
+ *  - The first call on a device looks up the array's device address (once
+ *    per device, with that device current); make that first call before any
+ *    stream capture.
+ *  - Every call shares the array: calls that overlap on the GPU (other
+ *    streams, other host threads) race on it and must be serialised by the
+ *    caller.  Nothing in it needs to start at zero (each call overwrites
+ *    every value it reads).
+ *  - stream: a cudaStream_t (NULL = the legacy default stream); the call
+ *    returns after its results are on the host.
+ * intr = {fx, fy, cx, cy} of the maps' pyramid level. */
+#define ODO_NOALLOC_MAX_PIXELS 1048576
+#define ODO_NOALLOC_SCRATCH_BYTES 139520
+int odo_icp_step_noalloc(const float *vmap_curr, const float *nmap_curr, const float *vmap_prev,
+                         const float *nmap_prev, size_t pitch_bytes, int cols, int rows, const float intr[4],
+                         float distThresh, float angleThresh, const float Rcurr[9], const float tcurr[3],
+                         const float Rprev_inv[9], const float tprev[3], void *stream, float matrixA[36],
+                         float vectorB[6], float residual[2]);
 
 #ifdef __cplusplus
 }

@@ -91,6 +91,9 @@ SIGNATURES = [
     ("odo_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
     ("odo_debug_profile", c_int, [c_void_p, P(c_double), c_int]),
     ("odo_debug_history", c_int, [c_void_p, P(c_double), c_int]),
+    ("odo_icp_step_noalloc", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, P(c_float),
+                                     c_float, c_float, P(c_float), P(c_float), P(c_float), P(c_float), c_void_p,
+                                     P(c_float), P(c_float), P(c_float)]),
 ]
 
 

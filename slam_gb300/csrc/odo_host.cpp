@@ -562,6 +562,7 @@ const char *odo_status_string(int status) {
         case ODO_ERR_STATE: return "call-order violation";
         case ODO_ERR_OOM: return "out of device memory";
         case ODO_ERR_TIMEOUT: return "device-side wait timed out";
+        case ODO_ERR_SIZE: return "image exceeds ODO_NOALLOC_MAX_PIXELS of the allocation-free entry point";
     }
     return "unknown status";
 }
