@@ -51,7 +51,15 @@ def parse():
     ap.add_argument("--mode", default="graph", choices=["graph", "stream", "persistent"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    return ap.parse_args()
+    ap.add_argument("--study", default=None, choices=[None, "batch", "precision"],
+                    help="batch: 512 mixed-resolution pairs per launch (batched verification); "
+                         "precision: 1000 corridor pairs, FP32 vs compensated FP32 vs the FP64 oracle")
+    ap.add_argument("--pairs", type=int, default=None)
+    ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
+    a = ap.parse_args()
+    if a.pairs is None:
+        a.pairs = 1000 if a.study == "precision" else 512
+    return a
 
 
 def dist_env():
@@ -333,8 +341,248 @@ def run_ours(args):
     return out
 
 
+def make_batch_pairs(n, seed):
+    """Mixed-resolution verification pairs: sizes uniform over
+    {160x120, 320x240, 640x480} (fx scaled), seeded rooms, motion <= 8 deg /
+    15 cm, 2-3 pyramid levels."""
+    from slam_gb300 import synth
+    rng = np.random.default_rng(seed)
+    sizes = [(160, 120), (320, 240), (640, 480)]
+    rooms = [synth.make_room(seed * 1000 + r, 20) for r in range(16)]
+    pairs = []
+    for i in range(n):
+        w, h = sizes[int(rng.integers(0, 3))]
+        p = synth.make_pair(seed * 100000 + i, cam=synth.Camera().scaled(w, h), max_deg=8.0, max_m=0.15,
+                            scene=rooms[i % 16])
+        p["levels"] = int(rng.integers(2, 4))
+        pairs.append(p)
+    return pairs
+
+
+def run_batch_study(args):
+    import torch
+    from slam_gb300 import synth
+    from slam_gb300.batch import BatchOdometry, FramePair, result_pose
+    torch.cuda.set_device(0)
+    t0 = time.time()
+    pairs = make_batch_pairs(args.pairs, args.seed)
+    gen_s = time.time() - t0
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    devd = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int16)).cuda().view(torch.uint16)
+    fps = [FramePair(p["cam"], dev(p["model_vert"]), dev(p["model_norm"]), dev(p["model_rgba"]), devd(p["depth"]),
+                     dev(p["rgba"]), dev(p["prev_rgba"]), p["T1"], levels=p["levels"]) for p in pairs]
+    stream = torch.cuda.current_stream()
+    b = BatchOdometry(len(fps), stream=stream.cuda_stream)
+    default_res = b.track(fps)
+    for _ in range(2):
+        b.track(fps)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    b.track(fps)
+    default_ms = (time.perf_counter() - t) * 1e3
+    default_poses = [result_pose(r) for r in default_res]
+    threads, ppt, tune_ms = b.autotune(fps)
+    descs = b._descs(fps)
+    for _ in range(max(args.warmup, 3)):
+        b.track(fps, descs=descs)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        res = b.track(fps, descs=descs)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    done = np.array([r.done_us for r in res])
+    err = [synth.pose_error(result_pose(r), p["T2"]) for r, p in zip(res, pairs)]
+    d_default = [synth.pose_error(result_pose(r), T) for r, T in zip(res, default_poses)]
+    differs = [k for k, d in enumerate(d_default) if d[0] > 1e-5 or d[1] > 1e-5]
+    # a pair "fails" when its tracked pose is off the ground truth by > 2 deg or 10 cm
+    failed = [k for k, e in enumerate(err) if e[0] > math.radians(2.0) or e[1] > 0.10]
+    px_iters = 0
+    for p in pairs:
+        n0 = p["cam"].width * p["cam"].height
+        px_iters += sum(it * (n0 >> (2 * l)) for l, it in enumerate([10, 5, 4][:p["levels"]]))
+    out = {"metric": "batched verification pairs/s (mixed 160x120-640x480, one CUDA graph)",
+           "value": len(pairs) / (ms * 1e-3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "data": "synthetic",
+           "config": {"workload": f"{len(pairs)} pairs per launch, sizes uniform over 160x120/320x240/640x480, "
+                                  "motion <= 8 deg / 15 cm, 2-3 levels, ICP+RGB, SO3 on",
+                      "autotuned_launch": {"threads": threads, "pixels_per_thread": ppt, "ms": tune_ms},
+                      "default_launch": {"threads": 256, "pixels_per_thread": 2, "ms_host_timed": default_ms},
+                      "generation_s": gen_s},
+           "pixel_iterations_per_step": px_iters,
+           "gpix_iter_per_s": px_iters / (ms * 1e-3) / 1e9,
+           "latency_us": {"p50": float(np.percentile(done, 50)), "p99": float(np.percentile(done, 99)),
+                          "batch_ms": ms,
+                          "note": "per pair: device time from the batch's first kernel to the end of the pair's "
+                                  "last Gauss-Newton solve; results reach the host with the whole batch"},
+           "pose_error_vs_gt": {"rot_rad_median": float(np.median([e[0] for e in err])),
+                                "trans_m_median": float(np.median([e[1] for e in err])),
+                                "failed_pairs": len(failed)},
+           "autotuned_vs_default_launch": {
+               "pairs_differing_over_1e-5": len(differs),
+               "of_which_failed": len(set(differs) & set(failed)),
+               "max_diff_converged_pairs": [max([d_default[k][0] for k in differs if k not in failed] + [0.0]),
+                                            max([d_default[k][1] for k in differs if k not in failed] + [0.0])]}}
+    print(json.dumps(out), flush=True)
+
+
+def _unpack29(v):
+    A = np.zeros((6, 6))
+    b = np.zeros(6)
+    k = 0
+    for i in range(6):
+        for j in range(i, 7):
+            if j == 6:
+                b[i] = v[k]
+            else:
+                A[i, j] = A[j, i] = v[k]
+            k += 1
+    return A, b
+
+
+PRECISION_FIELDS = ["pair", "cond", "inliers", "point", "relA_fp32", "relA_comp", "relb_fp32", "relb_comp",
+                    "inc_rot_fp32", "inc_rot_comp", "inc_trans_fp32", "inc_trans_comp", "count_diff_fp32",
+                    "count_diff_comp"]
+
+
+def precision_pair(i, seed, g32, gcomp, k64, cam, dist, angle):
+    """One corridor pair of the precision study: the ICP normal equations at
+    level 0 (at the start pose and at the FP64 oracle's converged pose) as the
+    tracker's FP32 and compensated-FP32 reductions deliver them, against the
+    FP64 oracle's on the same FP32 maps; the increments A^-1 b of each (one
+    FP64 LDLT, as the tracker's solve); the tracked poses against the FP64
+    oracle's tracking of the same raw frames."""
+    import torch
+    from slam_gb300 import synth
+    from oracle import oracle
+    p = synth.make_corridor_pair(seed * 100000 + i, cam=cam)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    devd = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int16)).cuda().view(torch.uint16)
+    T1 = p["T1"]
+    poses = {}
+    for name, g in (("fp32", g32), ("comp", gcomp)):
+        g.initFirstRGB(dev(p["prev_rgba"]))
+        g.initICPModel(dev(p["model_vert"]), dev(p["model_norm"]), 20.0, T1.astype(np.float32))
+        g.initRGBModel(dev(p["model_rgba"]))
+        g.initICP(devd(p["depth"]), 20.0)
+        g.initRGB(dev(p["rgba"]))
+        t, R = g.getIncrementalTransformation(T1[:3, 3].astype(np.float32), T1[:3, :3].astype(np.float32),
+                                              rgbOnly=False, icpWeight=10.0, pyramid=True, fastOdom=False, so3=True)
+        poses[name] = synth.pose(np.asarray(R, np.float64), np.asarray(t, np.float64))
+    o = oracle.Odometry(cam.width, cam.height, cam.cx, cam.cy, cam.fx, cam.fy, dist, angle, prec=64)
+    o.initFirstRGB(p["prev_rgba"])
+    o.initICPModel(p["model_vert"], p["model_norm"], 20.0, T1.astype(np.float32))
+    o.initRGBModel(p["model_rgba"])
+    o.initICP(p["depth"], 20.0)
+    o.initRGB(p["rgba"])
+    t64, R64 = o.getIncrementalTransformation(T1[:3, 3], T1[:3, :3], rgbOnly=False, icpWeight=10.0, pyramid=True,
+                                              fastOdom=False, so3=True)
+    T64 = synth.pose(np.asarray(R64, np.float64), np.asarray(t64, np.float64))
+    o.close()
+    maps = [g32.download(w, 0) for w in (1, 2, 3, 4)]
+    rows = []
+    Rp, tp = T1[:3, :3].astype(np.float32), T1[:3, 3].astype(np.float32)
+    Rpi = np.linalg.inv(Rp.astype(np.float64)).astype(np.float32)
+    for point, Tc in (("start", T1), ("converged", T64)):
+        Rc, tc = Tc[:3, :3].astype(np.float32), Tc[:3, 3].astype(np.float32)
+        s64, _, _ = k64.icp_step(Rc, tc, maps[0], maps[1], Rpi, tp, cam.fx, cam.fy, cam.cx, cam.cy, maps[2], maps[3],
+                                 dist, angle)
+        A64, b64 = _unpack29(s64)
+        x64 = oracle.ldlt_solve6(A64, b64)
+        row = {"pair": i, "cond": float(np.linalg.cond(A64)), "inliers": int(s64[28]), "point": point}
+        for name, g in (("fp32", g32), ("comp", gcomp)):
+            s = g.debug_icp_sums(0, Rc, tc, Rpi, tp)
+            A, b = _unpack29(s)
+            x = oracle.ldlt_solve6(A, b)
+            row["relA_" + name] = float(np.linalg.norm(A - A64) / np.linalg.norm(A64))
+            row["relb_" + name] = float(np.linalg.norm(b - b64) / max(np.linalg.norm(b64), 1e-300))
+            row["inc_trans_" + name] = float(np.linalg.norm(x[:3] - x64[:3]))
+            row["inc_rot_" + name] = float(np.linalg.norm(x[3:] - x64[3:]))
+            row["count_diff_" + name] = int(s[28] - s64[28])
+        rows.append(row)
+    pose_rows = {}
+    for name in ("fp32", "comp"):
+        pose_rows[name] = synth.pose_error(poses[name], T64)
+    pose_rows["fp64_vs_gt"] = synth.pose_error(T64, p["T2"])
+    pose_rows["fp32_vs_comp"] = synth.pose_error(poses["fp32"], poses["comp"])
+    return rows, pose_rows
+
+
+def run_precision_study(args):
+    """Precision study on low-texture corridor pairs (2 m x 20 m, floor-dominated
+    views, ~3 % of pixels on clutter): FP32 and compensated-FP32 JtJ/Jtr,
+    increments and tracked poses against the FP64 oracle (the oracle is the
+    checker here; nothing measured runs on it)."""
+    import csv
+    import torch
+    from slam_gb300 import synth, RGBDOdometry, PREC_COMPENSATED
+    from oracle import oracle
+    torch.cuda.set_device(0)
+    cam = synth.Camera()
+    from slam_gb300.odometry import DEFAULT_ANGLE_THRESH, DEFAULT_DIST_THRESH
+    dist, angle = DEFAULT_DIST_THRESH, DEFAULT_ANGLE_THRESH
+    g32 = RGBDOdometry(cam.width, cam.height, cam.cx, cam.cy, cam.fx, cam.fy, dist, angle)
+    gcomp = RGBDOdometry(cam.width, cam.height, cam.cx, cam.cy, cam.fx, cam.fy, dist, angle)
+    gcomp.set_precision(PREC_COMPENSATED)
+    k64 = oracle.Kernels(64)
+    t0 = time.time()
+    rows, poses = [], []
+    for i in range(args.pairs):
+        r, pr = precision_pair(i, args.seed, g32, gcomp, k64, cam, dist, angle)
+        rows += r
+        poses.append(pr)
+    elapsed = time.time() - t0
+    if args.pairs_out:
+        with open(args.pairs_out, "w", newline="") as f:
+            w = csv.writer(f)
+            w.writerow(PRECISION_FIELDS + ["pose_rot_fp32", "pose_trans_fp32", "pose_rot_comp", "pose_trans_comp",
+                                           "fp64_rot_vs_gt", "fp64_trans_vs_gt"])
+            for r in rows:
+                pr = poses[r["pair"]]
+                w.writerow([r[k] for k in PRECISION_FIELDS] + list(pr["fp32"]) + list(pr["comp"]) +
+                           list(pr["fp64_vs_gt"]))
+    pct = lambda v: {"p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90)),
+                     "p99": float(np.percentile(v, 99)), "max": float(np.max(v))}
+    summary = {}
+    for point in ("start", "converged"):
+        sel = [r for r in rows if r["point"] == point]
+        d = {"cond": {"p5": float(np.percentile([r["cond"] for r in sel], 5)),
+                      "p50": float(np.percentile([r["cond"] for r in sel], 50)),
+                      "p95": float(np.percentile([r["cond"] for r in sel], 95))},
+             "pairs_with_inlier_count_diff": int(sum(1 for r in sel if r["count_diff_fp32"] != 0))}
+        for name in ("fp32", "comp"):
+            d[name] = {k: pct([r[k + "_" + name] for r in sel]) for k in ("relA", "relb", "inc_rot", "inc_trans")}
+        summary[point] = d
+    pose = {}
+    for name in ("fp32", "comp"):
+        rot = np.array([p[name][0] for p in poses])
+        tr = np.array([p[name][1] for p in poses])
+        pose[name] = {"rot_rad": pct(rot), "trans_m": pct(tr),
+                      "frac_within_1e-5": float(np.mean((rot <= 1e-5) & (tr <= 1e-5)))}
+    pose["fp64_oracle_vs_ground_truth"] = {"rot_rad": pct([p["fp64_vs_gt"][0] for p in poses]),
+                                           "trans_m": pct([p["fp64_vs_gt"][1] for p in poses])}
+    pose["fp32_vs_comp"] = {"rot_rad": pct([p["fp32_vs_comp"][0] for p in poses]),
+                            "trans_m": pct([p["fp32_vs_comp"][1] for p in poses])}
+    out = {"study": "precision", "pairs": args.pairs, "data": "synthetic",
+           "config": {"workload": "low-texture corridor 2 m x 20 m, camera 1.5 m above the floor pitched down "
+                                  "25-40 deg, <= 3 deg / 5 cm relative motion, 640x480, 3 levels 10/5/4, "
+                                  "ICP+RGB (icpWeight 10), SO3 on",
+                      "jtj": "level-0 ICP sums at the start pose and at the FP64 oracle's converged pose; "
+                             "FP64 reference = oracle on the same FP32 maps"},
+           "jtj_increment": summary, "pose_vs_fp64_oracle": pose, "elapsed_s": elapsed}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.study == "batch":
+        run_batch_study(args)
+        return
+    if args.study == "precision":
+        run_precision_study(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -132,6 +132,62 @@ size_t odo_state_bytes(void);
 const char *odo_last_error(odo_t *h);
 const char *odo_status_string(int status);
 
+/* ---- batched tracking ----
+ * Many independent frame pairs of any sizes tracked together, e.g. the
+ * loop-closure candidate checks of the reference (Ferns::findFrame,
+ * src/lc/Ferns.cpp:237-279; model-to-model verification,
+ * src/apps/elastic_fusion_file.cpp:450-498).  For each pair the call does what
+ * initFirstRGB(prev_rgba) + initICPModel(model_verts, model_norms, cutoff,
+ * pose) + initRGBModel(model_rgba) + initICP(depth, cutoff) + initRGB(rgba) +
+ * getIncrementalTransformation(pose) do on one handle
+ * (src/odom/RGBDOdometryef.cpp:118-595), with the iteration schedule
+ * 10/5/4 restricted to the pair's first `levels` pyramid levels.  All pairs
+ * run in one CUDA graph; with the default launch shape every pair's result is
+ * bit-identical to the single-pair call. */
+typedef struct odo_batch odo_batch_t;
+
+typedef struct {
+    int width, height;           /* level-0 size, 16..8192 */
+    float fx, fy, cx, cy;
+    float distThresh, angleThresh; /* <= 0: reference defaults 0.10 m, sin(20 deg) */
+    float depthCutoff;           /* <= 0: 20 m (maxDepthProcessed, src/configs/ef_file.cfg:16) */
+    int levels;                  /* pyramid levels iterated, 1..3 */
+    const float *model_verts, *model_norms; /* RGBA32F, row pitch model_pitch */
+    size_t model_pitch;
+    const uint8_t *model_rgba;
+    size_t model_rgba_pitch;
+    const uint16_t *depth;       /* live depth, mm */
+    size_t depth_pitch;
+    const uint8_t *rgba;         /* live RGBA */
+    size_t rgba_pitch;
+    const uint8_t *prev_rgba;    /* previous live RGBA for the SO3 stage (may be NULL when so3 = 0) */
+    size_t prev_rgba_pitch;
+    float pose[16];              /* model pose = starting pose, row-major camera-to-world */
+} odo_pair;
+
+typedef struct {
+    float pose[16];              /* tracked pose */
+    float lastICPError, lastICPCount, lastRGBError, lastRGBCount, lastSO3Error, lastSO3Count;
+    int iterations[4];           /* SO3, level 0, level 1, level 2 */
+    double done_us;              /* time from the batch's first kernel to the end of this pair's last solve */
+    double lastA[36], lastb[6];
+} odo_pair_result;
+
+int odo_batch_create(int max_pairs, odo_batch_t **out);
+int odo_batch_destroy(odo_batch_t *b);
+int odo_batch_set_stream(odo_batch_t *b, void *stream);
+/* Launch shape of the two iteration kernels: threads per block (128 or 256)
+ * and pixels per thread (each pair gets ceil(pixels / (threads * ppt))
+ * blocks, at most 2 per SM).  Default 256 x 2 (the single-pair shape). */
+int odo_batch_set_launch(odo_batch_t *b, int threads, int pixels_per_thread);
+int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
+                    int so3, odo_pair_result *results);
+/* Times every launch shape on these pairs, keeps the fastest and returns it. */
+int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
+                       int so3, odo_pair_result *scratch_results, int *threads, int *pixels_per_thread,
+                       float *best_ms);
+const char *odo_batch_last_error(odo_batch_t *b);
+
 /* ---- parity / debugging access (used by the tests) ----
  * Buffer ids: 0 depth pyramid (u16), 1 vmap_curr, 2 nmap_curr, 3 vmap_prev,
  * 4 nmap_prev (planar float [3][rows][cols]), 5 lastDepth, 6 nextDepth
@@ -148,6 +204,17 @@ int odo_debug_upload(odo_t *h, int which, int level, const void *host_src, size_
  * partials). */
 int odo_debug_icp_step(odo_t *h, int level, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],
                        const float tprev[3], int32_t *assoc, double out29[29]);
+
+/* The ICP sums exactly as a tracking iteration hands them to the 6x6 solve:
+ * the same pass in the handle's precision (odo_set_precision), reduced
+ * across blocks in FP32 (or compensated FP32) in the tracker's order, then
+ * widened to FP64.  Used to measure summation error against an FP64 oracle. */
+int odo_debug_icp_sums(odo_t *h, int level, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],
+                       const float tprev[3], double out29[29]);
+
+/* The photometric sums of buffer 12 as a tracking iteration hands them to
+ * the solve (handle's precision, tracker's reduction order). */
+int odo_debug_rgb_sums(odo_t *h, int level, float sigma, double out29[29]);
 
 /* One photometric residual pass (computeRgbResidual, src/odom/reduce.cu:869-935)
  * writing buffer 12; out2 = {count, sum of squared differences (int32)}. */

@@ -59,6 +59,22 @@ class OdoStats(ctypes.Structure):
                 ("lastA", c_double * 36), ("lastb", c_double * 6)]
 
 
+class OdoPair(ctypes.Structure):
+    _fields_ = [("width", c_int), ("height", c_int), ("fx", c_float), ("fy", c_float), ("cx", c_float),
+                ("cy", c_float), ("distThresh", c_float), ("angleThresh", c_float), ("depthCutoff", c_float),
+                ("levels", c_int), ("model_verts", c_void_p), ("model_norms", c_void_p), ("model_pitch", c_size_t),
+                ("model_rgba", c_void_p), ("model_rgba_pitch", c_size_t), ("depth", c_void_p),
+                ("depth_pitch", c_size_t), ("rgba", c_void_p), ("rgba_pitch", c_size_t), ("prev_rgba", c_void_p),
+                ("prev_rgba_pitch", c_size_t), ("pose", c_float * 16)]
+
+
+class OdoPairResult(ctypes.Structure):
+    _fields_ = [("pose", c_float * 16), ("lastICPError", c_float), ("lastICPCount", c_float),
+                ("lastRGBError", c_float), ("lastRGBCount", c_float), ("lastSO3Error", c_float),
+                ("lastSO3Count", c_float), ("iterations", c_int * 4), ("done_us", c_double),
+                ("lastA", c_double * 36), ("lastb", c_double * 6)]
+
+
 # (name, restype, argtypes) of every function declared in include/slam_gb300.h
 SIGNATURES = [
     ("odo_create", c_int, [c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_float, P(c_void_p)]),
@@ -84,6 +100,8 @@ SIGNATURES = [
     ("odo_debug_upload", c_int, [c_void_p, c_int, c_int, c_void_p, c_size_t]),
     ("odo_debug_icp_step", c_int, [c_void_p, c_int, P(c_float), P(c_float), P(c_float), P(c_float), c_void_p,
                                    P(c_double)]),
+    ("odo_debug_icp_sums", c_int, [c_void_p, c_int, P(c_float), P(c_float), P(c_float), P(c_float), P(c_double)]),
+    ("odo_debug_rgb_sums", c_int, [c_void_p, c_int, c_float, P(c_double)]),
     ("odo_debug_rgb_residual", c_int, [c_void_p, c_int, P(c_float), P(c_float), P(ctypes.c_int32)]),
     ("odo_debug_rgb_step", c_int, [c_void_p, c_int, c_float, P(c_double)]),
     ("odo_debug_so3_step", c_int, [c_void_p, P(c_float), P(c_float), P(c_float), P(c_double)]),
@@ -91,6 +109,14 @@ SIGNATURES = [
     ("odo_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
     ("odo_debug_profile", c_int, [c_void_p, P(c_double), c_int]),
     ("odo_debug_history", c_int, [c_void_p, P(c_double), c_int]),
+    ("odo_batch_create", c_int, [c_int, P(c_void_p)]),
+    ("odo_batch_destroy", c_int, [c_void_p]),
+    ("odo_batch_set_stream", c_int, [c_void_p, c_void_p]),
+    ("odo_batch_set_launch", c_int, [c_void_p, c_int, c_int]),
+    ("odo_batch_track", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult)]),
+    ("odo_batch_autotune", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult),
+                                   P(c_int), P(c_int), P(c_float)]),
+    ("odo_batch_last_error", ctypes.c_char_p, [c_void_p]),
     ("odo_icp_step_noalloc", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, P(c_float),
                                      c_float, c_float, P(c_float), P(c_float), P(c_float), P(c_float), c_void_p,
                                      P(c_float), P(c_float), P(c_float)]),

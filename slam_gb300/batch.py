@@ -1,0 +1,104 @@
+"""Batched tracking of many independent frame pairs (C ABI odo_batch_*).
+
+Each pair does what initFirstRGB + initICPModel + initRGBModel + initICP +
+initRGB + getIncrementalTransformation do on one RGBDOdometry handle; all
+pairs run in one CUDA graph.  Inputs are CUDA tensors (see odometry.py)."""
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .odometry import OdometryError, _check_cuda_tensor
+
+
+class FramePair:
+    """Device inputs of one pair; `pose` is the model pose = starting pose."""
+
+    def __init__(self, cam, model_vert, model_norm, model_rgba, depth, rgba, prev_rgba, pose, levels=3):
+        self.cam, self.levels = cam, int(levels)
+        self.model_vert, self.model_norm, self.model_rgba = model_vert, model_norm, model_rgba
+        self.depth, self.rgba, self.prev_rgba = depth, rgba, prev_rgba
+        self.pose = np.asarray(pose, np.float32).reshape(4, 4)
+
+    def desc(self):
+        import torch
+        d = _native.OdoPair()
+        c = self.cam
+        d.width, d.height = c.width, c.height
+        d.fx, d.fy, d.cx, d.cy = c.fx, c.fy, c.cx, c.cy
+        d.distThresh = d.angleThresh = d.depthCutoff = 0.0
+        d.levels = self.levels
+        d.model_pitch = _check_cuda_tensor(self.model_vert, torch.float32, (4,), "model_vert")
+        d.model_verts, d.model_norms = self.model_vert.data_ptr(), self.model_norm.data_ptr()
+        d.model_rgba = self.model_rgba.data_ptr()
+        d.model_rgba_pitch = _check_cuda_tensor(self.model_rgba, torch.uint8, (4,), "model_rgba")
+        d.depth = self.depth.data_ptr()
+        d.depth_pitch = _check_cuda_tensor(self.depth, torch.uint16, (), "depth")
+        d.rgba = self.rgba.data_ptr()
+        d.rgba_pitch = _check_cuda_tensor(self.rgba, torch.uint8, (4,), "rgba")
+        if self.prev_rgba is not None:
+            d.prev_rgba = self.prev_rgba.data_ptr()
+            d.prev_rgba_pitch = _check_cuda_tensor(self.prev_rgba, torch.uint8, (4,), "prev_rgba")
+        for k in range(16):
+            d.pose[k] = float(self.pose.reshape(16)[k])
+        return d
+
+
+class BatchOdometry:
+    def __init__(self, max_pairs, stream=None):
+        self._L = _native.load()
+        h = ctypes.c_void_p()
+        rc = self._L.odo_batch_create(int(max_pairs), ctypes.byref(h))
+        if rc != 0:
+            raise OdometryError(rc, "odo_batch_create failed")
+        self._h = h
+        self.max_pairs = int(max_pairs)
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+        self._check(self._L.odo_batch_set_stream(self._h, ctypes.c_void_p(stream)), "odo_batch_set_stream")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise OdometryError(rc, "%s: %s %s" % (what, self._L.odo_status_string(rc).decode(),
+                                                   self._L.odo_batch_last_error(self._h).decode()))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.odo_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_launch(self, threads, pixels_per_thread):
+        self._check(self._L.odo_batch_set_launch(self._h, int(threads), int(pixels_per_thread)), "set_launch")
+
+    def _descs(self, pairs):
+        arr = (_native.OdoPair * len(pairs))()
+        for i, p in enumerate(pairs):
+            arr[i] = p.desc()
+        return arr
+
+    def track(self, pairs, rgbOnly=False, icpWeight=10.0, fastOdom=False, so3=True, descs=None):
+        descs = descs if descs is not None else self._descs(pairs)
+        res = (_native.OdoPairResult * len(pairs))()
+        self._check(self._L.odo_batch_track(self._h, descs, len(pairs), int(bool(rgbOnly)), float(icpWeight),
+                                            int(bool(fastOdom)), int(bool(so3)), res), "odo_batch_track")
+        return res
+
+    def autotune(self, pairs, rgbOnly=False, icpWeight=10.0, fastOdom=False, so3=True):
+        descs = self._descs(pairs)
+        res = (_native.OdoPairResult * len(pairs))()
+        t, p, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        self._check(self._L.odo_batch_autotune(self._h, descs, len(pairs), int(bool(rgbOnly)), float(icpWeight),
+                                               int(bool(fastOdom)), int(bool(so3)), res, ctypes.byref(t),
+                                               ctypes.byref(p), ctypes.byref(ms)), "odo_batch_autotune")
+        return t.value, p.value, ms.value
+
+
+def result_pose(r):
+    return np.array(r.pose, np.float64).reshape(4, 4)

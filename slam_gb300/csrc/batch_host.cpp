@@ -1,0 +1,574 @@
+// Batched tracking: many independent frame pairs (e.g. loop-closure
+// candidate verification, src/lc/Ferns.cpp:237-279, or model-to-model checks,
+// src/apps/elastic_fusion_file.cpp:450-498) of uneven resolutions tracked in
+// one CUDA graph.  Every stage of a single-pair call runs as one batched launch
+// over all pairs (the pair is a grid coordinate), so the per-pixel arithmetic,
+// the reductions and the per-iteration solve are exactly the single-pair
+// path's; with the default launch shape each pair's result is bit-identical to
+// odo_get_incremental_transformation on the same inputs.  An autotuner picks
+// the block size and pixels per thread of the two iteration kernels.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/slam_gb300.h"
+#include "odo_internal.h"
+#include "se3_math.h"
+
+using namespace slamgb;
+
+namespace {
+
+inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct PairBufs {
+    int w = 0, h = 0;
+    int dims_w[kLevels], dims_h[kLevels];
+    size_t off = 0;  // offset of this pair's storage in the pixel arena
+    // device pointers (carved from the arena)
+    Img<uint16_t> depth[kLevels];
+    Map3 vc[kLevels], nc[kLevels], vp[kLevels], np[kLevels];
+    Img<float> dep[kLevels];  // photometric depth (last == next: both come from the model vertices)
+    Img<uint8_t> last[kLevels], next[kLevels], lastnext[kLevels];
+    Img<int16_t> dx[kLevels], dy[kLevels];
+    Img<Corr> corr[kLevels];
+    Img<uint8_t> cand[kLevels];
+    Img<float> vz;
+    ReduceWs ws;
+};
+
+using Layout = std::vector<std::tuple<int, int>>;
+using GKey = std::tuple<int, int, int, int, int, int, int, int>;
+
+}  // namespace
+
+struct odo_batch {
+    int max_pairs = 0;
+    int device = 0, sm_count = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    // pixel arena (per-pair buffers) and argument arena
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    Layout layout;
+    std::vector<PairBufs> bufs;
+    unsigned char *args_dev = nullptr, *args_host = nullptr;  // host pinned
+    size_t args_bytes = 0;
+    TrackState *st_dev = nullptr, *st_host = nullptr;           // host pinned
+    // offsets of the argument blocks in the argument arena
+    size_t o_model, o_rgbd[3], o_gauss[3][2], o_pyr[2], o_vn, o_deriv, o_so3, o_pass[kLevels];
+    int threads = 256, ppt = 2;
+    int max_nb[kLevels];
+    int max_w = 0, max_h = 0;
+    std::map<GKey, cudaGraphExec_t> graphs;
+    std::string last_error;
+};
+
+namespace {
+
+int bfail(odo_batch_t *b, cudaError_t e, const char *what) {
+    if (b) {
+        char buf[256];
+        std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+        b->last_error = buf;
+    }
+    return e == cudaErrorMemoryAllocation ? ODO_ERR_OOM : ODO_ERR_CUDA;
+}
+
+#define BCK(call)                                          \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return bfail(b, e_, #call); \
+    } while (0)
+
+void drop_graphs(odo_batch_t *b) {
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+}
+
+template <typename T>
+Img<T> carve_img(unsigned char *base, size_t &off, int cols, int rows) {
+    Img<T> im;
+    im.cols = cols;
+    im.rows = rows;
+    im.pitch = round_up((size_t)cols * sizeof(T), 256);
+    im.data = (T *)(base + off);
+    off += im.pitch * rows;
+    return im;
+}
+Map3 carve_map(unsigned char *base, size_t &off, int cols, int rows) {
+    Map3 m;
+    m.cols = cols;
+    m.rows = rows;
+    m.pitch = round_up((size_t)cols * sizeof(float), 256);
+    m.data = (float *)(base + off);
+    off += m.pitch * rows * 3;
+    return m;
+}
+
+int blocks_for(const odo_batch_t *b, int n) {
+    int per = b->threads * b->ppt;
+    int nb = (n + per - 1) / per;
+    if (nb > 2 * b->sm_count) nb = 2 * b->sm_count;
+    return nb < 1 ? 1 : nb;
+}
+
+// (Re)builds the per-pair buffers for a new list of image sizes.
+int ensure_layout(odo_batch_t *b, const odo_pair *pairs, int n) {
+    Layout lay;
+    for (int i = 0; i < n; ++i) lay.emplace_back(pairs[i].width, pairs[i].height);
+    if (lay == b->layout && b->arena) return ODO_OK;
+    BCK(cudaStreamSynchronize(b->stream));
+    drop_graphs(b);
+    if (b->arena) cudaFree(b->arena);
+    b->arena = nullptr;
+    b->bufs.assign(n, PairBufs());
+    // pass 1: sizes
+    size_t total = 0;
+    const int maxb = 2 * b->sm_count;
+    b->max_w = b->max_h = 0;
+    for (int i = 0; i < n; ++i) {
+        PairBufs &p = b->bufs[i];
+        p.w = pairs[i].width;
+        p.h = pairs[i].height;
+        if (p.w > b->max_w) b->max_w = p.w;
+        if (p.h > b->max_h) b->max_h = p.h;
+        p.off = total;
+        size_t off = 0;
+        unsigned char *nul = nullptr;
+        for (int l = 0; l < kLevels; ++l) {
+            int w = p.w >> l, h = p.h >> l;
+            p.dims_w[l] = w;
+            p.dims_h[l] = h;
+            carve_img<uint16_t>(nul, off, w, h);
+            for (int k = 0; k < 4; ++k) carve_map(nul, off, w, h);
+            carve_img<float>(nul, off, w, h);
+            for (int k = 0; k < 3; ++k) carve_img<uint8_t>(nul, off, w, h);
+            carve_img<int16_t>(nul, off, w, h);
+            carve_img<int16_t>(nul, off, w, h);
+            carve_img<Corr>(nul, off, w, h);
+            carve_img<uint8_t>(nul, off, w, h);
+        }
+        carve_img<float>(nul, off, p.w, p.h);
+        off = round_up(off, 256) + round_up(sizeof(float) * 32 * maxb, 256) * 2 +
+              round_up(sizeof(int) * 2 * maxb, 256) + 256;
+        total += round_up(off, 256);
+    }
+    cudaError_t e = cudaMalloc(&b->arena, total ? total : 256);
+    if (e != cudaSuccess) return bfail(b, e, "cudaMalloc(batch arena)");
+    b->arena_bytes = total;
+    BCK(cudaMemset(b->arena, 0, total ? total : 256));
+    // pass 2: carve
+    for (int i = 0; i < n; ++i) {
+        PairBufs &p = b->bufs[i];
+        unsigned char *base = (unsigned char *)b->arena + p.off;
+        size_t off = 0;
+        for (int l = 0; l < kLevels; ++l) {
+            int w = p.dims_w[l], h = p.dims_h[l];
+            p.depth[l] = carve_img<uint16_t>(base, off, w, h);
+            p.vc[l] = carve_map(base, off, w, h);
+            p.nc[l] = carve_map(base, off, w, h);
+            p.vp[l] = carve_map(base, off, w, h);
+            p.np[l] = carve_map(base, off, w, h);
+            p.dep[l] = carve_img<float>(base, off, w, h);
+            p.last[l] = carve_img<uint8_t>(base, off, w, h);
+            p.next[l] = carve_img<uint8_t>(base, off, w, h);
+            p.lastnext[l] = carve_img<uint8_t>(base, off, w, h);
+            p.dx[l] = carve_img<int16_t>(base, off, w, h);
+            p.dy[l] = carve_img<int16_t>(base, off, w, h);
+            p.corr[l] = carve_img<Corr>(base, off, w, h);
+            p.cand[l] = carve_img<uint8_t>(base, off, w, h);
+        }
+        p.vz = carve_img<float>(base, off, p.w, p.h);
+        off = round_up(off, 256);
+        p.ws.icp_part = (float *)(base + off);
+        off += round_up(sizeof(float) * 32 * maxb, 256);
+        p.ws.rgb_part = (float *)(base + off);
+        off += round_up(sizeof(float) * 32 * maxb, 256);
+        p.ws.res_part = (int *)(base + off);
+        off += round_up(sizeof(int) * 2 * maxb, 256);
+        p.ws.counters = (unsigned *)(base + off);
+        p.ws.max_blocks = maxb;
+    }
+    b->layout = lay;
+    return ODO_OK;
+}
+
+// Writes every per-pair argument block into the pinned argument arena.
+void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float icpWeight, int fastOdom, int so3) {
+    unsigned char *H = b->args_host;
+    auto at = [&](size_t o) { return H + o; };
+    const int icp = !rgbOnly && icpWeight > 0;
+    const int rgb = rgbOnly || icpWeight < 100;
+    for (int i = 0; i < kLevels; ++i) b->max_nb[i] = 1;
+    for (int i = 0; i < n; ++i) {
+        const odo_pair &q = pairs[i];
+        PairBufs &p = b->bufs[i];
+        const Intr K0{q.fx, q.fy, q.cx, q.cy};
+        auto intr = [&](int l) {
+            int div = 1 << l;
+            return Intr{K0.fx / div, K0.fy / div, K0.cx / div, K0.cy / div};
+        };
+        // model maps (initICPModel): planar pyramid + transform by the model pose
+        ModelArgs m{};
+        m.v4 = q.model_verts;
+        m.n4 = q.model_norms;
+        m.pitch4 = q.model_pitch;
+        m.cols0 = p.w;
+        m.rows0 = p.h;
+        for (int l = 0; l < kLevels; ++l) {
+            m.vmap[l] = p.vp[l];
+            m.nmap[l] = p.np[l];
+        }
+        m.do_transform = 1;
+        const float Rp[9] = {q.pose[0], q.pose[1], q.pose[2], q.pose[4], q.pose[5], q.pose[6], q.pose[8], q.pose[9],
+                             q.pose[10]};
+        for (int k = 0; k < 9; ++k) m.R[k] = Rp[k];
+        m.t[0] = q.pose[3];
+        m.t[1] = q.pose[7];
+        m.t[2] = q.pose[11];
+        m.vz = p.vz.data;
+        m.vz_pitch = p.vz.pitch;
+        std::memcpy(at(b->o_model) + i * sizeof(ModelArgs), &m, sizeof(m));
+        // photometric level 0: model image + depth from the model vertices,
+        // live image, previous live image (SO3)
+        const uint8_t *src[3] = {q.model_rgba, q.rgba, q.prev_rgba ? q.prev_rgba : q.rgba};
+        const size_t sp[3] = {q.model_rgba_pitch, q.rgba_pitch, q.prev_rgba ? q.prev_rgba_pitch : q.rgba_pitch};
+        Img<uint8_t> *imgs[3] = {p.last, p.next, p.lastnext};
+        for (int r = 0; r < 3; ++r) {
+            RgbdArgs a{p.vz.data, p.vz.pitch, src[r], sp[r], p.dep[0], imgs[r][0], r == 0 ? 1 : 0};
+            std::memcpy(at(b->o_rgbd[r]) + i * sizeof(RgbdArgs), &a, sizeof(a));
+            for (int l = 0; l < 2; ++l) {
+                Img<const float> ds{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
+                Img<const uint8_t> is{imgs[r][l].data, imgs[r][l].pitch, imgs[r][l].cols, imgs[r][l].rows};
+                GaussArgs g{ds, p.dep[l + 1], is, imgs[r][l + 1], r == 0 ? 1 : 0};
+                std::memcpy(at(b->o_gauss[r][l]) + i * sizeof(GaussArgs), &g, sizeof(g));
+            }
+        }
+        // depth pyramid (the level-0 input is read in place)
+        for (int l = 0; l < 2; ++l) {
+            Img<const uint16_t> s0 = l == 0 ? Img<const uint16_t>{q.depth, q.depth_pitch, p.w, p.h}
+                                            : Img<const uint16_t>{p.depth[l].data, p.depth[l].pitch, p.depth[l].cols,
+                                                                  p.depth[l].rows};
+            PyrArgs a{s0, p.depth[l + 1]};
+            std::memcpy(at(b->o_pyr[l]) + i * sizeof(PyrArgs), &a, sizeof(a));
+        }
+        VNArgs v{};
+        for (int l = 0; l < kLevels; ++l) {
+            v.depth[l] = l == 0 ? Img<const uint16_t>{q.depth, q.depth_pitch, p.w, p.h}
+                                : Img<const uint16_t>{p.depth[l].data, p.depth[l].pitch, p.depth[l].cols,
+                                                      p.depth[l].rows};
+            v.vmap[l] = p.vc[l];
+            v.nmap[l] = p.nc[l];
+            const Intr K = intr(l);
+            v.fx_inv[l] = 1.f / K.fx;
+            v.fy_inv[l] = 1.f / K.fy;
+            v.cx[l] = K.cx;
+            v.cy[l] = K.cy;
+        }
+        v.cutoff = q.depthCutoff > 0 ? q.depthCutoff : 20.0f;  // maxDepthProcessed (src/configs/ef_file.cfg:16)
+        std::memcpy(at(b->o_vn) + i * sizeof(VNArgs), &v, sizeof(v));
+        DerivArgs d{};
+        const float minGrad[kLevels] = {5, 3, 1};
+        const float sobelScale = (float)(1.0 / pow(2.0, 3));
+        for (int l = 0; l < kLevels; ++l) {
+            d.src[l] = Img<const uint8_t>{p.next[l].data, p.next[l].pitch, p.next[l].cols, p.next[l].rows};
+            d.dx[l] = p.dx[l];
+            d.dy[l] = p.dy[l];
+            d.depth[l] = Img<const float>{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
+            d.cand[l] = p.cand[l];
+            d.minScale[l] = (float)(pow(minGrad[l], 2.0) / pow((double)sobelScale, 2.0));
+        }
+        std::memcpy(at(b->o_deriv) + i * sizeof(DerivArgs), &d, sizeof(d));
+        So3Args so{b->st_dev + i,
+                   Img<const uint8_t>{p.lastnext[2].data, p.lastnext[2].pitch, p.lastnext[2].cols, p.lastnext[2].rows},
+                   Img<const uint8_t>{p.next[2].data, p.next[2].pitch, p.next[2].cols, p.next[2].rows}, intr(2)};
+        std::memcpy(at(b->o_so3) + i * sizeof(So3Args), &so, sizeof(so));
+        // iteration schedule (src/odom/RGBDOdometryef.cpp:382-384), restricted to `levels`
+        const int base[kLevels] = {fastOdom ? 3 : 10, 5, 4};
+        for (int l = 0; l < kLevels; ++l) {
+            PassArgs a{};
+            LevelArgs &L = a.L;
+            L.level = l;
+            L.cols = p.dims_w[l];
+            L.rows = p.dims_h[l];
+            L.K = intr(l);
+            L.vmap_curr = p.vc[l];
+            L.nmap_curr = p.nc[l];
+            L.vmap_prev = p.vp[l];
+            L.nmap_prev = p.np[l];
+            L.angleThres = q.angleThresh > 0 ? q.angleThresh : 0.34202015f;
+            L.distThres = q.distThresh > 0 ? q.distThresh : 0.10f;
+            L.dIdx = Img<const int16_t>{p.dx[l].data, p.dx[l].pitch, p.dx[l].cols, p.dx[l].rows};
+            L.dIdy = Img<const int16_t>{p.dy[l].data, p.dy[l].pitch, p.dy[l].cols, p.dy[l].rows};
+            L.lastDepth = Img<const float>{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
+            L.nextDepth = L.lastDepth;
+            L.lastImage = Img<const uint8_t>{p.last[l].data, p.last[l].pitch, p.last[l].cols, p.last[l].rows};
+            L.nextImage = Img<const uint8_t>{p.next[l].data, p.next[l].pitch, p.next[l].cols, p.next[l].rows};
+            L.corr = p.corr[l];
+            L.cand = Img<const uint8_t>{p.cand[l].data, p.cand[l].pitch, p.cand[l].cols, p.cand[l].rows};
+            L.minScale = d.minScale[l];
+            L.maxDepthDelta = 0.07f;
+            L.sobelScale = sobelScale;
+            a.st = b->st_dev + i;
+            a.ws = p.ws;
+            a.iters = (l < q.levels) ? base[l] : 0;
+            const int npx = L.cols * L.rows;
+            a.nb_icp = a.iters ? blocks_for(b, npx) : 0;
+            a.nb_rgb = a.iters ? (rgb ? a.nb_icp : 1) : 0;
+            a.invFx = 1.0f / L.K.fx;
+            a.invFy = 1.0f / L.K.fy;
+            a.km = make_kmats(L.K);
+            if (a.nb_icp > b->max_nb[l]) b->max_nb[l] = a.nb_icp;
+            std::memcpy(at(b->o_pass[l]) + i * sizeof(PassArgs), &a, sizeof(a));
+        }
+        // initial state of the call (src/odom/RGBDOdometryef.cpp:278-282)
+        TrackState &st = b->st_host[i];
+        std::memset(&st, 0, sizeof(st));
+        for (int k = 0; k < 9; ++k) st.Rprev[k] = Rp[k];
+        st.tprev[0] = q.pose[3];
+        st.tprev[1] = q.pose[7];
+        st.tprev[2] = q.pose[11];
+        st.icpWeight = icpWeight;
+        st.rgbOnly = rgbOnly ? 1 : 0;
+        st.icp = icp;
+        st.rgb = rgb;
+        st.so3 = so3 ? 1 : 0;
+        for (int k = 0; k < 9; ++k) st.resultR[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        st.lastICPCount = st.lastRGBCount = st.lastSO3Count = (float)(p.w * p.h);
+    }
+}
+
+cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, const int max_iters[kLevels]) {
+    cudaStream_t s = b->stream;
+    cudaError_t e = cudaMemcpyAsync(b->args_dev, b->args_host, b->args_bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
+    auto A = [&](size_t o) { return (const void *)(b->args_dev + o); };
+    const int W = b->max_w, Hh = b->max_h;
+    if (e == cudaSuccess) e = launch_stamp_batch(b->st_dev, n, s);
+    if (e == cudaSuccess) e = launch_model_maps_batch((const ModelArgs *)A(b->o_model), n, W, Hh, s);
+    const int roles = so3 ? 3 : 2;
+    for (int r = 0; r < roles && e == cudaSuccess; ++r)
+        e = launch_rgbd_level0_batch((const RgbdArgs *)A(b->o_rgbd[r]), n, W, Hh, s);
+    for (int l = 0; l < 2 && e == cudaSuccess; ++l)
+        for (int r = 0; r < roles && e == cudaSuccess; ++r)
+            e = launch_gauss_down_batch((const GaussArgs *)A(b->o_gauss[r][l]), n, W >> (l + 1), Hh >> (l + 1), s);
+    for (int l = 0; l < 2 && e == cudaSuccess; ++l)
+        e = launch_pyr_down_depth_batch((const PyrArgs *)A(b->o_pyr[l]), n, W >> (l + 1), Hh >> (l + 1), s);
+    if (e == cudaSuccess) e = launch_vmap_nmap_batch((const VNArgs *)A(b->o_vn), n, W, Hh, s);
+    if (e == cudaSuccess && rgb) e = launch_derivatives_batch((const DerivArgs *)A(b->o_deriv), n, W, Hh, s);
+    if (e == cudaSuccess && so3) e = launch_so3_batch((const So3Args *)A(b->o_so3), n, s);
+    if (e == cudaSuccess) e = launch_track_begin_batch(b->st_dev, n, s);
+    for (int l = kLevels - 1; l >= 0 && e == cudaSuccess; --l)
+        for (int j = 0; j < max_iters[l] && e == cudaSuccess; ++j)
+            e = launch_level_iteration_batch((const PassArgs *)A(b->o_pass[l]), n, b->max_nb[l],
+                                             rgb ? b->max_nb[l] : 1, b->threads, 0, j, s);
+    if (e == cudaSuccess) e = launch_track_end_batch(b->st_dev, n, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_host, b->st_dev, sizeof(TrackState) * n, cudaMemcpyDeviceToHost, s);
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int odo_batch_create(int max_pairs, odo_batch_t **out) {
+    if (!out || max_pairs < 1 || max_pairs > 65535) return ODO_ERR_ARG;
+    *out = nullptr;
+    odo_batch_t *b = new (std::nothrow) odo_batch_t();
+    if (!b) return ODO_ERR_OOM;
+    b->max_pairs = max_pairs;
+    auto bail = [&](cudaError_t e, const char *what) {
+        int rc = bfail(b, e, what);
+        odo_batch_destroy(b);
+        return rc;
+    };
+    cudaError_t e;
+    if ((e = cudaGetDevice(&b->device)) != cudaSuccess) return bail(e, "cudaGetDevice");
+    if ((e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device)) != cudaSuccess)
+        return bail(e, "cudaDeviceGetAttribute");
+    if ((e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(e, "cudaStreamCreate");
+    b->stream = b->own_stream;
+    // argument arena layout
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t r = o;
+        o = round_up(o + bytes, 256);
+        return r;
+    };
+    const size_t np = (size_t)max_pairs;
+    b->o_model = take(np * sizeof(ModelArgs));
+    for (int r = 0; r < 3; ++r) b->o_rgbd[r] = take(np * sizeof(RgbdArgs));
+    for (int r = 0; r < 3; ++r)
+        for (int l = 0; l < 2; ++l) b->o_gauss[r][l] = take(np * sizeof(GaussArgs));
+    for (int l = 0; l < 2; ++l) b->o_pyr[l] = take(np * sizeof(PyrArgs));
+    b->o_vn = take(np * sizeof(VNArgs));
+    b->o_deriv = take(np * sizeof(DerivArgs));
+    b->o_so3 = take(np * sizeof(So3Args));
+    for (int l = 0; l < kLevels; ++l) b->o_pass[l] = take(np * sizeof(PassArgs));
+    b->args_bytes = o;
+    if ((e = cudaMalloc(&b->args_dev, o)) != cudaSuccess) return bail(e, "cudaMalloc(args)");
+    if ((e = cudaMallocHost(&b->args_host, o)) != cudaSuccess) return bail(e, "cudaMallocHost(args)");
+    std::memset(b->args_host, 0, o);
+    if ((e = cudaMalloc(&b->st_dev, sizeof(TrackState) * np)) != cudaSuccess) return bail(e, "cudaMalloc(states)");
+    if ((e = cudaMallocHost(&b->st_host, sizeof(TrackState) * np)) != cudaSuccess)
+        return bail(e, "cudaMallocHost(states)");
+    *out = b;
+    return ODO_OK;
+}
+
+int odo_batch_destroy(odo_batch_t *b) {
+    if (!b) return ODO_ERR_ARG;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graphs(b);
+    if (b->arena) cudaFree(b->arena);
+    if (b->args_dev) cudaFree(b->args_dev);
+    if (b->args_host) cudaFreeHost(b->args_host);
+    if (b->st_dev) cudaFree(b->st_dev);
+    if (b->st_host) cudaFreeHost(b->st_host);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    delete b;
+    return ODO_OK;
+}
+
+int odo_batch_set_stream(odo_batch_t *b, void *stream) {
+    if (!b) return ODO_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->own_stream;
+    if (s != b->stream) {
+        BCK(cudaStreamSynchronize(b->stream));
+        drop_graphs(b);
+        b->stream = s;
+    }
+    return ODO_OK;
+}
+
+int odo_batch_set_launch(odo_batch_t *b, int threads, int pixels_per_thread) {
+    if (!b || (threads != 128 && threads != 256) || pixels_per_thread < 1 || pixels_per_thread > 64)
+        return ODO_ERR_ARG;
+    if (threads != b->threads || pixels_per_thread != b->ppt) drop_graphs(b);
+    b->threads = threads;
+    b->ppt = pixels_per_thread;
+    return ODO_OK;
+}
+
+int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
+                    int so3, odo_pair_result *results) {
+    if (!b || !pairs || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
+    for (int i = 0; i < npairs; ++i) {
+        const odo_pair &q = pairs[i];
+        if (q.width < 16 || q.height < 16 || q.width > 8192 || q.height > 8192 || q.levels < 1 || q.levels > 3 ||
+            !q.model_verts || !q.model_norms || !q.model_rgba || !q.depth || !q.rgba ||
+            q.model_pitch < (size_t)q.width * 16 || q.depth_pitch < (size_t)q.width * 2 ||
+            q.rgba_pitch < (size_t)q.width * 4 || q.model_rgba_pitch < (size_t)q.width * 4 || !(q.fx != 0) ||
+            !(q.fy != 0))
+            return ODO_ERR_ARG;
+    }
+    int rc = ensure_layout(b, pairs, npairs);
+    if (rc != ODO_OK) return rc;
+    const int rgb = rgbOnly || icpWeight < 100;
+    build_args(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3);
+    int max_iters[kLevels] = {0, 0, 0};
+    int maxlev = 0;
+    for (int i = 0; i < npairs; ++i)
+        if (pairs[i].levels > maxlev) maxlev = pairs[i].levels;
+    const int base[kLevels] = {fastOdom ? 3 : 10, 5, 4};
+    for (int l = 0; l < maxlev; ++l) max_iters[l] = base[l];
+    GKey key{npairs, rgb, so3 ? 1 : 0, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt};
+    auto it = b->graphs.find(key);
+    if (it == b->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, max_iters);
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return bfail(b, e, "enqueue_batch (capture)");
+        }
+        if (e2 != cudaSuccess) return bfail(b, e2, "cudaStreamEndCapture");
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bfail(b, e, "cudaGraphInstantiate");
+        it = b->graphs.emplace(key, ex).first;
+    }
+    BCK(cudaGraphLaunch(it->second, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < npairs; ++i) {
+        const TrackState &st = b->st_host[i];
+        if (st.status != 0) return st.status;
+        odo_pair_result &r = results[i];
+        for (int a = 0; a < 3; ++a) {
+            for (int c = 0; c < 3; ++c) r.pose[a * 4 + c] = st.out_R[a * 3 + c];
+            r.pose[a * 4 + 3] = st.out_t[a];
+        }
+        r.pose[12] = r.pose[13] = r.pose[14] = 0.f;
+        r.pose[15] = 1.f;
+        r.lastICPError = st.lastICPError;
+        r.lastICPCount = st.lastICPCount;
+        r.lastRGBError = st.lastRGBError;
+        r.lastRGBCount = st.lastRGBCount;
+        r.lastSO3Error = st.lastSO3Error;
+        r.lastSO3Count = st.lastSO3Count;
+        r.iterations[0] = st.so3_iters;
+        for (int l = 0; l < kLevels; ++l) r.iterations[1 + l] = st.iters_run[l];
+        r.done_us = (double)((st.t_solve ? st.t_solve : st.t_end) - st.t_start) * 1e-3;
+        std::memcpy(r.lastA, st.lastA, sizeof(r.lastA));
+        std::memcpy(r.lastb, st.lastb, sizeof(r.lastb));
+    }
+    return ODO_OK;
+}
+
+int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
+                       int so3, odo_pair_result *scratch_results, int *threads, int *pixels_per_thread,
+                       float *best_ms) {
+    if (!b || !threads || !pixels_per_thread) return ODO_ERR_ARG;
+    const int cand_t[2] = {128, 256};
+    const int cand_p[4] = {1, 2, 4, 8};
+    float best = 1e30f;
+    int bt = b->threads, bp = b->ppt;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    for (int ti = 0; ti < 2; ++ti)
+        for (int pi = 0; pi < 4; ++pi) {
+            int rc = odo_batch_set_launch(b, cand_t[ti], cand_p[pi]);
+            if (rc == ODO_OK) rc = odo_batch_track(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3, scratch_results);
+            if (rc != ODO_OK) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return rc;
+            }
+            float ms = 0;
+            BCK(cudaEventRecord(e0, b->stream));
+            for (int r = 0; r < 2 && rc == ODO_OK; ++r)
+                rc = odo_batch_track(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3, scratch_results);
+            BCK(cudaEventRecord(e1, b->stream));
+            BCK(cudaEventSynchronize(e1));
+            BCK(cudaEventElapsedTime(&ms, e0, e1));
+            ms /= 2;
+            if (rc == ODO_OK && ms < best) {
+                best = ms;
+                bt = cand_t[ti];
+                bp = cand_p[pi];
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int rc = odo_batch_set_launch(b, bt, bp);
+    *threads = bt;
+    *pixels_per_thread = bp;
+    if (best_ms) *best_ms = best;
+    return rc;
+}
+
+const char *odo_batch_last_error(odo_batch_t *b) { return b ? b->last_error.c_str() : ""; }
+
+}  // extern "C"

@@ -593,6 +593,29 @@ int odo_debug_icp_step(odo_t *h, int level, const float Rcurr[9], const float tc
     return ODO_OK;
 }
 
+int odo_debug_icp_sums(odo_t *h, int level, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],
+                       const float tprev[3], double out29[29]) {
+    if (!h || level < 0 || level >= kLevels || !Rcurr || !tcurr || !Rprev_inv || !tprev || !out29) return ODO_ERR_ARG;
+    LevelArgs L = level_args(h, level);
+    TrackLaunch c = h->cfg[level];
+    c.precision = h->precision;
+    CK(launch_debug_icp_sums(L, Rcurr, tcurr, Rprev_inv, tprev, h->dbg_dev, h->ws, c, h->stream));
+    CK(cudaMemcpyAsync(out29, h->dbg_dev, 29 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ODO_OK;
+}
+
+int odo_debug_rgb_sums(odo_t *h, int level, float sigma, double out29[29]) {
+    if (!h || level < 0 || level >= kLevels || !out29) return ODO_ERR_ARG;
+    LevelArgs L = level_args(h, level);
+    TrackLaunch c = h->cfg[level];
+    c.precision = h->precision;
+    CK(launch_debug_rgb_sums(L, sigma, h->dbg_dev, h->ws, c, h->stream));
+    CK(cudaMemcpyAsync(out29, h->dbg_dev, 29 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ODO_OK;
+}
+
 int odo_debug_rgb_residual(odo_t *h, int level, const float krkinv[9], const float kt[3], int32_t out2[2]) {
     if (!h || level < 0 || level >= kLevels || !krkinv || !kt || !out2) return ODO_ERR_ARG;
     LevelArgs L = level_args(h, level);

@@ -65,6 +65,9 @@ struct TrackState {
     // increment x[0..5]
     int nhist;
     double hist[32][9];
+    unsigned long long t_begin, t_end;  // device globaltimer at the start / end of the call
+    unsigned long long t_start;         // batch: globaltimer when the batch's first kernel ran
+    unsigned long long t_solve;         // globaltimer at the end of the pair's last Gauss-Newton solve
     // output
     float out_R[9], out_t[3];
 };
@@ -96,6 +99,62 @@ struct ReduceWs {
     int max_blocks;
 };
 
+// ---- per-image argument blocks of the preprocessing kernels (one per
+// frame pair; the batched launchers take device arrays of them) ----
+struct PyrArgs {
+    Img<const uint16_t> src;
+    Img<uint16_t> dst;
+};
+struct VNArgs {
+    Img<const uint16_t> depth[kLevels];
+    Map3 vmap[kLevels], nmap[kLevels];
+    float fx_inv[kLevels], fy_inv[kLevels], cx[kLevels], cy[kLevels];
+    float cutoff;
+};
+struct ModelArgs {
+    const float *v4, *n4;
+    size_t pitch4;
+    int cols0, rows0;
+    Map3 vmap[kLevels], nmap[kLevels];
+    int do_transform;
+    float R[9], t[3];
+    float *vz;
+    size_t vz_pitch;
+};
+struct RgbdArgs {
+    const float *vz;
+    size_t vz_pitch;
+    const uint8_t *rgba;
+    size_t rgba_pitch;
+    Img<float> depth0;
+    Img<uint8_t> img0;
+    int do_depth;
+};
+struct GaussArgs {
+    Img<const float> dsrc;
+    Img<float> ddst;
+    Img<const uint8_t> isrc;
+    Img<uint8_t> idst;
+    int do_depth;
+};
+struct DerivArgs {
+    Img<const uint8_t> src[kLevels];
+    Img<int16_t> dx[kLevels], dy[kLevels];
+    Img<const float> depth[kLevels];
+    Img<uint8_t> cand[kLevels];
+    float minScale[kLevels];
+};
+
+// Batched launches: `args` is a device array of npairs blocks; the grid
+// covers the largest image (max_cols x max_rows at level 0), blocks outside a
+// smaller pair's image return at once.
+cudaError_t launch_pyr_down_depth_batch(const PyrArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s);
+cudaError_t launch_vmap_nmap_batch(const VNArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s);
+cudaError_t launch_model_maps_batch(const ModelArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s);
+cudaError_t launch_rgbd_level0_batch(const RgbdArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s);
+cudaError_t launch_gauss_down_batch(const GaussArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s);
+cudaError_t launch_derivatives_batch(const DerivArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s);
+
 // ---- launchers: preprocessing (odo_maps.cu) ----
 cudaError_t launch_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst, cudaStream_t s);
 cudaError_t launch_vmap_nmap(const Img<const uint16_t> *depth, const Map3 *vmap, const Map3 *nmap, const Intr *K,
@@ -112,6 +171,29 @@ cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t>
                                int nlevels, cudaStream_t s);
 
 // ---- launchers: tracking (odo_track.cu) ----
+// FP64 intrinsics and inverse of one pyramid level (computed on the host).
+struct KMats {
+    double K[9], Kinv[9];
+};
+
+// One pair's arguments of the two per-iteration kernels at one level.
+struct PassArgs {
+    LevelArgs L;
+    TrackState *st;
+    ReduceWs ws;
+    int nb_icp, nb_rgb;  // blocks of this pair in the two kernels (0: level unused)
+    int iters;           // iterations of this pair at this level
+    float invFx, invFy;
+    KMats km;
+};
+
+// One pair's SO3 inputs (level 2 images and intrinsics).
+struct So3Args {
+    TrackState *st;
+    Img<const uint8_t> last, next;
+    Intr K2;
+};
+
 struct TrackLaunch {
     int blocks_icp;    // grid of the association/reduction kernel
     int blocks_rgb;    // grid of the photometric reduction kernel
@@ -128,11 +210,26 @@ cudaError_t launch_track_end(TrackState *st, cudaStream_t s);
 cudaError_t launch_iteration_part(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg, int iter,
                                   int which, cudaStream_t s);
 int persistent_max_blocks(int threads);
+KMats make_kmats(const Intr &K);
+
+// batched tracking launches (pair = blockIdx.y of the pass kernels, one
+// thread-block cluster per pair for SO3); `states` is a device array
+cudaError_t launch_track_begin_batch(TrackState *states, int npairs, cudaStream_t s);
+cudaError_t launch_stamp_batch(TrackState *states, int npairs, cudaStream_t s);
+cudaError_t launch_track_end_batch(TrackState *states, int npairs, cudaStream_t s);
+cudaError_t launch_so3_batch(const So3Args *args, int npairs, cudaStream_t s);
+cudaError_t launch_level_iteration_batch(const PassArgs *args, int npairs, int max_nb_icp, int max_nb_rgb,
+                                         int threads, int precision, int iter, cudaStream_t s);
 
 // debug single passes
 cudaError_t launch_debug_icp(const LevelArgs &L, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],
                              const float tprev[3], int32_t *assoc, double *out29_dev, ReduceWs ws,
                              const TrackLaunch &cfg, cudaStream_t s);
+cudaError_t launch_debug_icp_sums(const LevelArgs &L, const float Rcurr[9], const float tcurr[3],
+                                  const float Rprev_inv[9], const float tprev[3], double *out29_dev, ReduceWs ws,
+                                  const TrackLaunch &cfg, cudaStream_t s);
+cudaError_t launch_debug_rgb_sums(const LevelArgs &L, float sigma, double *out29_dev, ReduceWs ws,
+                                  const TrackLaunch &cfg, cudaStream_t s);
 cudaError_t launch_debug_rgb_residual(const LevelArgs &L, const float krkinv[9], const float kt[3], int *out2_dev,
                                       ReduceWs ws, const TrackLaunch &cfg, cudaStream_t s);
 cudaError_t launch_debug_rgb_step(const LevelArgs &L, float sigma, double *out29_dev, ReduceWs ws,

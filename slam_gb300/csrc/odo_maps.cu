@@ -17,9 +17,9 @@ namespace {
 constexpr int BX = 32, BY = 8;
 
 // pyrDownGaussKernel, src/odom/utils.cu:57-94 (sigma_color = 30, :103).
-__global__ void k_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void pyr_px(const PyrArgs &a, int x, int y) {
+    const Img<const uint16_t> src = a.src;
+    const Img<uint16_t> dst = a.dst;
     if (x >= dst.cols || y >= dst.rows) return;
     const int D = 5;
     const float sigma_color = 30.f;
@@ -42,6 +42,12 @@ __global__ void k_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst) {
     }
     at(dst, x, y) = static_cast<int>(sum / wall);
 }
+__global__ void k_pyr_down_depth(PyrArgs a) {
+    pyr_px(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+__global__ void k_pyr_down_depth_b(const PyrArgs *A) {
+    pyr_px(A[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
 
 // computeVmapKernel, src/odom/utils.cu:109-133, for one pixel.
 __device__ __forceinline__ float3 vertex_at(const Img<const uint16_t> &depth, int u, int v, float fx_inv,
@@ -55,22 +61,12 @@ __device__ __forceinline__ float3 vertex_at(const Img<const uint16_t> &depth, in
     return make_float3(qnan_f(), qnan_f(), qnan_f());
 }
 
-struct VNArgs {
-    Img<const uint16_t> depth[kLevels];
-    Map3 vmap[kLevels], nmap[kLevels];
-    float fx_inv[kLevels], fy_inv[kLevels], cx[kLevels], cy[kLevels];
-    float cutoff;
-};
-
 // createVMap + createNMap (src/odom/utils.cu:109-204) fused, all levels in
 // one launch (blockIdx.z = level).  The normal needs the vertices right and
 // below; they are recomputed from depth with the same arithmetic instead of
 // being re-read, so the result is bit-identical to the two-pass version.
-__global__ void k_vmap_nmap(VNArgs a) {
-    const int l = blockIdx.z;
+__device__ __forceinline__ void vnmap_px(const VNArgs &a, int l, int u, int v) {
     const Img<const uint16_t> depth = a.depth[l];
-    int u = blockIdx.x * blockDim.x + threadIdx.x;
-    int v = blockIdx.y * blockDim.y + threadIdx.y;
     if (u >= depth.cols || v >= depth.rows) return;
     const float fxi = a.fx_inv[l], fyi = a.fy_inv[l], cx = a.cx[l], cy = a.cy[l];
     const Map3 vm = a.vmap[l], nm = a.nmap[l];
@@ -89,18 +85,13 @@ __global__ void k_vmap_nmap(VNArgs a) {
     map_row(nm, 1, v)[u] = n.y;
     map_row(nm, 2, v)[u] = n.z;
 }
-
-struct ModelArgs {
-    const float *v4, *n4;
-    size_t pitch4;
-    int cols0, rows0;
-    Map3 vmap[kLevels], nmap[kLevels];
-    int do_transform;
-    M33 R;
-    float3 t;
-    float *vz;
-    size_t vz_pitch;
-};
+__global__ void k_vmap_nmap(VNArgs a) {
+    vnmap_px(a, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+__global__ void k_vmap_nmap_b(const VNArgs *A) {
+    vnmap_px(A[blockIdx.z / kLevels], blockIdx.z % kLevels, blockIdx.x * blockDim.x + threadIdx.x,
+             blockIdx.y * blockDim.y + threadIdx.y);
+}
 
 // copyMapsKernel (src/odom/utils.cu:270-310): a pixel is valid iff the
 // vertex z != 0.
@@ -145,11 +136,8 @@ __device__ __forceinline__ void level1_px(const ModelArgs &a, int x, int y, floa
 // copyMaps, resizeVMap/NMap x2 and tranformMaps for every level in one
 // launch (blockIdx.z = level); level l re-derives its 2^l x 2^l block from
 // the RGBA32F input with the reference's order of operations.
-__global__ void k_model_maps(ModelArgs a) {
-    const int l = blockIdx.z;
+__device__ __forceinline__ void model_px(const ModelArgs &a, int l, int x, int y) {
     const Map3 vm = a.vmap[l], nm = a.nmap[l];
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= vm.cols || y >= vm.rows) return;
     float3 v, n;
     if (l == 0) {
@@ -170,8 +158,10 @@ __global__ void k_model_maps(ModelArgs a) {
         // tranformMapsKernel, src/odom/utils.cu:206-248
         const float q = qnan_f();
         float3 vd = make_float3(q, q, q), nd = make_float3(q, q, q);
-        if (!isnan(v.x)) vd = a.R * v + a.t;
-        if (!isnan(n.x)) nd = a.R * n;
+        const M33 R = load_m33(a.R);
+        const float3 t = make_float3(a.t[0], a.t[1], a.t[2]);
+        if (!isnan(v.x)) vd = R * v + t;
+        if (!isnan(n.x)) nd = R * n;
         v = vd;
         n = nd;
     }
@@ -182,23 +172,33 @@ __global__ void k_model_maps(ModelArgs a) {
     map_row(nm, 1, y)[x] = n.y;
     map_row(nm, 2, y)[x] = n.z;
 }
+__global__ void k_model_maps(ModelArgs a) {
+    model_px(a, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+__global__ void k_model_maps_b(const ModelArgs *A) {
+    model_px(A[blockIdx.z / kLevels], blockIdx.z % kLevels, blockIdx.x * blockDim.x + threadIdx.x,
+             blockIdx.y * blockDim.y + threadIdx.y);
+}
 
 // verticesToDepthKernel (src/odom/utils.cu:526-537, cut at maxDepthRGB =
 // 6.0, src/odom/RGBDOdometryef.cpp:37) and bgr2IntensityKernel
 // (src/odom/utils.cu:550-563; RGBA input, so R is weighted 0.114).
-__global__ void k_rgbd_level0(const float *vz, size_t vz_pitch, const uint8_t *rgba, size_t rgba_pitch, Img<float> depth0,
-                              Img<uint8_t> img0, int do_depth) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= img0.cols || y >= img0.rows) return;
-    if (do_depth) {
+__device__ __forceinline__ void rgbd_px(const RgbdArgs &a, int x, int y) {
+    if (x >= a.img0.cols || y >= a.img0.rows) return;
+    if (a.do_depth) {
         const float cutOff = 6.0f;
-        float z = rowp(vz, vz_pitch, y)[x];
-        at(depth0, x, y) = z > cutOff || z <= 0 ? qnan_f() : z;
+        float z = rowp(a.vz, a.vz_pitch, y)[x];
+        at(a.depth0, x, y) = z > cutOff || z <= 0 ? qnan_f() : z;
     }
-    uchar4 src = *reinterpret_cast<const uchar4 *>(rowp(rgba, rgba_pitch, y) + 4 * x);
+    uchar4 src = *reinterpret_cast<const uchar4 *>(rowp(a.rgba, a.rgba_pitch, y) + 4 * x);
     int value = (float)src.x * 0.114f + (float)src.y * 0.299f + (float)src.z * 0.587f;
-    at(img0, x, y) = value;
+    at(a.img0, x, y) = value;
+}
+__global__ void k_rgbd_level0(RgbdArgs a) {
+    rgbd_px(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+__global__ void k_rgbd_level0_b(const RgbdArgs *A) {
+    rgbd_px(A[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 __constant__ float c_gauss5x5[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36, 24, 6, 4, 16, 24, 16, 4, 1, 4, 6, 4, 1};
@@ -207,10 +207,12 @@ __constant__ float c_gauss5x5[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36,
 // pyrDownKernelIntensityGauss (src/odom/utils.cu:470-500) in one launch:
 // masked 5x5 Gaussian, window clamped at cols-1/rows-1 (exclusive), reversed
 // kernel index, int count.
-__global__ void k_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const uint8_t> isrc, Img<uint8_t> idst,
-                             int do_depth) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void gauss_px(const GaussArgs &a, int x, int y) {
+    const Img<const float> dsrc = a.dsrc;
+    const Img<float> ddst = a.ddst;
+    const Img<const uint8_t> isrc = a.isrc;
+    const Img<uint8_t> idst = a.idst;
+    const int do_depth = a.do_depth;
     if (x >= idst.cols || y >= idst.rows) return;
     const int D = 5;
     int tx = min(2 * x - D / 2 + D, isrc.cols - 1);
@@ -245,19 +247,17 @@ __global__ void k_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const u
         at(idst, x, y) = (sum / (float)count);
     }
 }
+__global__ void k_gauss_down(GaussArgs a) {
+    gauss_px(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+__global__ void k_gauss_down_b(const GaussArgs *A) {
+    gauss_px(A[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
 
 __constant__ float c_sobel_x[9] = {0.52201f, 0.00000f, -0.52201f, 0.79451f, -0.00000f,
                                    -0.79451f, 0.52201f, 0.00000f, -0.52201f};
 __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.00000f,
                                    0.00000f, -0.52201f, -0.79451f, -0.52201f};
-
-struct DerivArgs {
-    Img<const uint8_t> src[kLevels];
-    Img<int16_t> dx[kLevels], dy[kLevels];
-    Img<const float> depth[kLevels];
-    Img<uint8_t> cand[kLevels];
-    float minScale[kLevels];
-};
 
 // applyKernel (src/odom/utils.cu:582-606), all levels in one launch.  Also
 // evaluates, once per frame, the pose-independent preconditions of a
@@ -265,11 +265,8 @@ struct DerivArgs {
 // src/odom/reduce.cu:782-810: j0 < cols-5, i < rows-1, no zero intensity in
 // the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
 // into a byte mask, so the per-iteration pass reads one byte per pixel.
-__global__ void k_derivatives(DerivArgs a) {
-    const int l = blockIdx.z;
+__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, int x, int y) {
     const Img<const uint8_t> src = a.src[l];
-    int x = threadIdx.x + blockIdx.x * blockDim.x;
-    int y = threadIdx.y + blockIdx.y * blockDim.y;
     if (x >= src.cols || y >= src.rows) return;
     float dxVal = 0, dyVal = 0;
     int kernelIndex = 8;
@@ -299,13 +296,20 @@ __global__ void k_derivatives(DerivArgs a) {
     }
     at(a.cand[l], x, y) = c ? 1 : 0;
 }
+__global__ void k_derivatives(DerivArgs a) {
+    deriv_px(a, blockIdx.z, threadIdx.x + blockIdx.x * blockDim.x, threadIdx.y + blockIdx.y * blockDim.y);
+}
+__global__ void k_derivatives_b(const DerivArgs *A) {
+    deriv_px(A[blockIdx.z / kLevels], blockIdx.z % kLevels, threadIdx.x + blockIdx.x * blockDim.x,
+             threadIdx.y + blockIdx.y * blockDim.y);
+}
 
 inline dim3 grid2(int cols, int rows, int z = 1) { return dim3((cols + BX - 1) / BX, (rows + BY - 1) / BY, z); }
 
 }  // namespace
 
 cudaError_t launch_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst, cudaStream_t s) {
-    k_pyr_down_depth<<<grid2(dst.cols, dst.rows), dim3(BX, BY), 0, s>>>(src, dst);
+    k_pyr_down_depth<<<grid2(dst.cols, dst.rows), dim3(BX, BY), 0, s>>>(PyrArgs{src, dst});
     return cudaGetLastError();
 }
 
@@ -340,8 +344,8 @@ cudaError_t launch_model_maps(const float *v4, const float *n4, size_t pitch4, i
         a.nmap[l] = nmap[l];
     }
     a.do_transform = do_transform;
-    for (int i = 0; i < 3; ++i) a.R.r[i] = make_float3(R[3 * i], R[3 * i + 1], R[3 * i + 2]);
-    a.t = make_float3(t[0], t[1], t[2]);
+    for (int i = 0; i < 9; ++i) a.R[i] = R[i];
+    for (int i = 0; i < 3; ++i) a.t[i] = t[i];
     a.vz = vz;
     a.vz_pitch = vz_pitch;
     k_model_maps<<<grid2(cols, rows, nlevels), dim3(BX, BY), 0, s>>>(a);
@@ -350,13 +354,14 @@ cudaError_t launch_model_maps(const float *v4, const float *n4, size_t pitch4, i
 
 cudaError_t launch_rgbd_level0(const float *vz, size_t vz_pitch, const uint8_t *rgba, size_t rgba_pitch, int cols,
                                int rows, Img<float> depth0, Img<uint8_t> img0, int do_depth, cudaStream_t s) {
-    k_rgbd_level0<<<grid2(cols, rows), dim3(BX, BY), 0, s>>>(vz, vz_pitch, rgba, rgba_pitch, depth0, img0, do_depth);
+    k_rgbd_level0<<<grid2(cols, rows), dim3(BX, BY), 0, s>>>(
+        RgbdArgs{vz, vz_pitch, rgba, rgba_pitch, depth0, img0, do_depth});
     return cudaGetLastError();
 }
 
 cudaError_t launch_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const uint8_t> isrc, Img<uint8_t> idst,
                               int do_depth, cudaStream_t s) {
-    k_gauss_down<<<grid2(idst.cols, idst.rows), dim3(BX, BY), 0, s>>>(dsrc, ddst, isrc, idst, do_depth);
+    k_gauss_down<<<grid2(idst.cols, idst.rows), dim3(BX, BY), 0, s>>>(GaussArgs{dsrc, ddst, isrc, idst, do_depth});
     return cudaGetLastError();
 }
 
@@ -373,6 +378,31 @@ cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t>
         a.minScale[l] = minScale[l];
     }
     k_derivatives<<<grid2(src[0].cols, src[0].rows, nlevels), dim3(BX, BY), 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pyr_down_depth_batch(const PyrArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
+    k_pyr_down_depth_b<<<grid2(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    return cudaGetLastError();
+}
+cudaError_t launch_vmap_nmap_batch(const VNArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
+    k_vmap_nmap_b<<<grid2(max_cols, max_rows, npairs * kLevels), dim3(BX, BY), 0, s>>>(args);
+    return cudaGetLastError();
+}
+cudaError_t launch_model_maps_batch(const ModelArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
+    k_model_maps_b<<<grid2(max_cols, max_rows, npairs * kLevels), dim3(BX, BY), 0, s>>>(args);
+    return cudaGetLastError();
+}
+cudaError_t launch_rgbd_level0_batch(const RgbdArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
+    k_rgbd_level0_b<<<grid2(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    return cudaGetLastError();
+}
+cudaError_t launch_gauss_down_batch(const GaussArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
+    k_gauss_down_b<<<grid2(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    return cudaGetLastError();
+}
+cudaError_t launch_derivatives_batch(const DerivArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
+    k_derivatives_b<<<grid2(max_cols, max_rows, npairs * kLevels), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 

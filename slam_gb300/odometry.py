@@ -202,6 +202,21 @@ class RGBDOdometry:
                     "debug_icp_step")
         return out, (assoc.reshape(h, w) if want_assoc else None)
 
+    def debug_icp_sums(self, level, Rcurr, tcurr, Rprev_inv, tprev):
+        """The 29 ICP sums as a tracking iteration hands them to the solve
+        (handle precision, tracker reduction order)."""
+        f = lambda a, n: np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(n))
+        Rc, tc, Ri, tp = f(Rcurr, 9), f(tcurr, 3), f(Rprev_inv, 9), f(tprev, 3)
+        out = np.zeros(29, dtype=np.float64)
+        self._check(self._L.odo_debug_icp_sums(self._h, level, _fptr(Rc), _fptr(tc), _fptr(Ri), _fptr(tp),
+                                               _dptr(out)), "debug_icp_sums")
+        return out
+
+    def debug_rgb_sums(self, level, sigma):
+        out = np.zeros(29, dtype=np.float64)
+        self._check(self._L.odo_debug_rgb_sums(self._h, level, float(sigma), _dptr(out)), "debug_rgb_sums")
+        return out
+
     def debug_rgb_residual(self, level, krkinv, kt):
         k = np.ascontiguousarray(np.asarray(krkinv, dtype=np.float32).reshape(9))
         t = np.ascontiguousarray(np.asarray(kt, dtype=np.float32).reshape(3))

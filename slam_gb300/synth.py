@@ -134,6 +134,35 @@ def room_camera(rng):
     return pose(Ry @ Rx @ Rz, t)
 
 
+def corridor_camera(rng):
+    """A camera about 1.5 m above the corridor floor, looking along the
+    corridor and pitched down 25-40 degrees so the floor plane fills most of
+    the image."""
+    yaw = math.radians(rng.uniform(-12, 12)) + (math.pi if rng.uniform() < 0.5 else 0.0)
+    pitch = -math.radians(rng.uniform(25, 40))
+    roll = math.radians(rng.uniform(-3, 3))
+    R = rotvec_to_R([0, yaw, 0]) @ rotvec_to_R([pitch, 0, 0]) @ rotvec_to_R([0, 0, roll])
+    t = np.array([rng.uniform(-0.4, 0.4), rng.uniform(-0.15, 0.15), rng.uniform(-5.0, 5.0)])
+    return pose(R, t)
+
+
+def make_corridor_pair(seed, cam=None, max_deg=3.0, max_m=0.05, nclutter=24, tex_amp=None):
+    """One frame pair of the precision study: a low-texture corridor seen
+    from corridor_camera, live frame at a relative motion <= max_deg/max_m."""
+    cam = cam or Camera()
+    rng = np.random.default_rng(seed + 0x5151)
+    scene = make_corridor(seed, nclutter)
+    if tex_amp is not None:
+        scene.tex_amp = tex_amp
+    T1 = corridor_camera(rng)
+    T2 = T1 @ random_motion(rng, max_deg, max_m)
+    model = render(scene, T1, cam, depth=False, rgba=True, model=True)
+    live = render(scene, T2, cam, noise_seed=seed * 7919 + 1, depth=True, rgba=True, model=False)
+    prev = render(scene, T1, cam, noise_seed=seed * 7919 + 2, depth=False, rgba=True, model=False)
+    return {"cam": cam, "T1": T1, "T2": T2, "model_vert": model["vert"], "model_norm": model["norm"],
+            "model_rgba": model["rgba"], "depth": live["depth"], "rgba": live["rgba"], "prev_rgba": prev["rgba"]}
+
+
 def pose_error(T_est, T_gt):
     """(rotation error rad, translation error m)."""
     D = np.linalg.inv(T_gt) @ T_est
