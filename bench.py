@@ -56,6 +56,7 @@ def parse():
                          "precision: 1000 corridor pairs, FP32 vs compensated FP32 vs the FP64 oracle")
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
+    ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
     a = ap.parse_args()
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
@@ -381,7 +382,10 @@ def run_batch_study(args):
     b.track(fps)
     default_ms = (time.perf_counter() - t) * 1e3
     default_poses = [result_pose(r) for r in default_res]
-    threads, ppt, tune_ms = b.autotune(fps)
+    if args.no_autotune:
+        threads, ppt, tune_ms = 256, 2, default_ms
+    else:
+        threads, ppt, tune_ms = b.autotune(fps)
     descs = b._descs(fps)
     for _ in range(max(args.warmup, 3)):
         b.track(fps, descs=descs)

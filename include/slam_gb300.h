@@ -152,6 +152,7 @@ typedef struct {
     float distThresh, angleThresh; /* <= 0: reference defaults 0.10 m, sin(20 deg) */
     float depthCutoff;           /* <= 0: 20 m (maxDepthProcessed, src/configs/ef_file.cfg:16) */
     int levels;                  /* pyramid levels iterated, 1..3 */
+    int iterations[3];           /* per-level Gauss-Newton iterations (0: the reference's 10 (3 fastOdom) / 5 / 4), <= 20 */
     const float *model_verts, *model_norms; /* RGBA32F, row pitch model_pitch */
     size_t model_pitch;
     const uint8_t *model_rgba;
@@ -182,6 +183,13 @@ int odo_batch_set_stream(odo_batch_t *b, void *stream);
 int odo_batch_set_launch(odo_batch_t *b, int threads, int pixels_per_thread);
 int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
                     int so3, odo_pair_result *results);
+/* As odo_batch_track, but every pair starts from its own motion estimate
+ * instead of the SO3 pre-alignment: init_dev[i] (device, 6 floats:
+ * translation m, rotation vector rad) is the live camera's motion in the
+ * model camera's frame, so tracking starts at pose * exp(init) (no
+ * counterpart in the reference; used by the learned warm start). */
+int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init_dev, int rgbOnly,
+                         float icpWeight, int fastOdom, odo_pair_result *results);
 /* Times every launch shape on these pairs, keeps the fastest and returns it. */
 int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
                        int so3, odo_pair_result *scratch_results, int *threads, int *pixels_per_thread,
@@ -285,6 +293,56 @@ int odo_icp_step_noalloc(const float *vmap_curr, const float *nmap_curr, const f
                          float distThresh, float angleThresh, const float Rcurr[9], const float tcurr[3],
                          const float Rprev_inv[9], const float tprev[3], void *stream, float matrixA[36],
                          float vectorB[6], float residual[2]);
+
+/* ---- Learned warm start (no counterpart in the reference) ----
+ * A BF16 CNN that proposes the coarse SE(3) motion of a frame pair from both
+ * frames' 160x120 depth and gray images; forward and backward products run
+ * on the tcgen05 tensor cores (FP32 accumulation).
+ * Input [B][120][160][8] FP16 NHWC: model depth (m), model gray (0..1), live
+ * depth (m), live gray, four zero channels.  Output [B][6]: translation (m)
+ * and rotation vector (rad) of the live camera in the model camera's frame.
+ * Six 3x3/stride-2 convolutions (8->32->64->128->128->128->128, ReLU), fc
+ * 768->768 (ReLU), fc 768->6; odo_cnn_param_count() FP32 parameters.
+ * Loss: mean over the batch of sum_i (scale_i (out_i - label_i))^2, Adam. */
+typedef struct odo_cnn odo_cnn_t;
+size_t odo_cnn_param_count(void);
+int odo_cnn_create(int max_batch, odo_cnn_t **out);
+int odo_cnn_destroy(odo_cnn_t *n);
+int odo_cnn_set_stream(odo_cnn_t *n, void *stream);
+int odo_cnn_init_params(odo_cnn_t *n, uint64_t seed);          /* He-normal weights, zero biases */
+int odo_cnn_set_params(odo_cnn_t *n, const float *host_params); /* also resets the optimiser */
+int odo_cnn_get_params(odo_cnn_t *n, float *host_params);
+int odo_cnn_set_loss_scale(odo_cnn_t *n, const float scale[6]);
+/* out_dev (may be NULL): [batch][6] FP32 on the device */
+int odo_cnn_forward(odo_cnn_t *n, const uint16_t *input_dev, int batch, float *out_dev);
+/* Network inputs [npairs][120][160][8] of frame pairs whose level-0 size is
+ * (160 s) x (120 s): s x s block means of the model depth (vertex z) and
+ * intensity and of the live depth and intensity (asynchronous, on the
+ * network's stream). */
+int odo_cnn_pack_input(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t *input_dev);
+/* forward + loss + backward + Adam (beta 0.9/0.999, eps 1e-8); loss_host may be NULL (no sync) */
+int odo_cnn_train_step(odo_cnn_t *n, const uint16_t *input_dev, const float *labels_dev, int batch, float lr,
+                       float *loss_host);
+/* forward + loss + backward without an update; gradients in the parameter layout */
+int odo_cnn_gradients(odo_cnn_t *n, const uint16_t *input_dev, const float *labels_dev, int batch,
+                      float *grad_host, float *loss_host);
+const char *odo_cnn_last_error(odo_cnn_t *n);
+/* GPU ray caster of the synthetic test scenes (scene struct of the synthetic
+ * data generator, synth_scene): view i of scene view_scene[i] at
+ * camera-to-world pose poses[16 i .. 16 i + 15] (row-major), depth noise
+ * seed noise_seeds[i]; outputs (device, any may be NULL) stacked per view:
+ * depth mm [n][h][w], RGBA [n][h][w][4], camera-frame vertices and normals
+ * RGBA32F [n][h][w][4].  Synchronous on `stream`. */
+int odo_synth_render(const void *scenes_host, int nscenes, const int *view_scene, const float *poses,
+                     const uint64_t *noise_seeds, int n, int w, int h, float fx, float fy, float cx, float cy,
+                     float noise_k, float dropout, int min_mm, int max_mm, uint16_t *depth_dev, uint8_t *rgba_dev,
+                     float *vert_dev, float *norm_dev, void *stream);
+/* C[M][N] (FP32) = A[M][K] B[N][K]^T with BF16 A, B (rows padded to a
+ * multiple of 8 elements) on the tensor-core GEMM; bn = tile width 32..256,
+ * layout = 0 (the library's operand layout) or 1 (offsets exchanged; a
+ * self-check of the layout). */
+int odo_cnn_debug_gemm(const uint16_t *A_dev, const uint16_t *B_dev, float *C_dev, int M, int N, int K, int bn,
+                       int layout, void *stream);
 
 #ifdef __cplusplus
 }

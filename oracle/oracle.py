@@ -334,3 +334,31 @@ class Odometry:
         size = int(np.prod(spec[1])) * dt.itemsize
         buf = (ctypes.c_char * size).from_address(ptr)
         return np.frombuffer(buf, dtype=dt).reshape(spec[1]).copy()
+
+
+# ---------------------------------------------------------------- warm-start network
+def cnn_layout():
+    w = (ctypes.c_size_t * 8)()
+    b = (ctypes.c_size_t * 8)()
+    t = ctypes.c_size_t()
+    lib().cnn_layout(w, b, ctypes.byref(t))
+    return list(w), list(b), t.value
+
+
+def cnn_run(params, inputs_f16, labels, scale, rounding=True, want_grad=True):
+    """Forward + loss (+ gradients) of the warm-start network on the CPU.
+    params: FP32 parameter vector; inputs_f16: uint16 [B,120,160,8] (FP16
+    bits); labels [B,6].  Returns (out [B,6], loss, grad or None)."""
+    p = np.ascontiguousarray(params, np.float64)
+    x = np.ascontiguousarray(inputs_f16, np.uint16)
+    B = x.shape[0]
+    lab = np.ascontiguousarray(labels, np.float64).reshape(B, 6)
+    sc = np.ascontiguousarray(scale, np.float64).reshape(6)
+    out = np.zeros((B, 6), np.float64)
+    loss = ctypes.c_double()
+    grad = np.zeros_like(p) if want_grad else None
+    f = lib().cnn_oracle_run
+    f.restype = ctypes.c_int
+    f(_p(p), x.ctypes.data_as(ctypes.c_void_p), _p(lab), _p(sc), ctypes.c_int(B), ctypes.c_int(int(bool(rounding))),
+      _p(out), ctypes.byref(loss), _p(grad) if want_grad else None)
+    return out, loss.value, grad

@@ -4,7 +4,7 @@
                                        + C++ host driver + C ABI
   slam_gb300/_lib/libslam_synth.so  -- synthetic RGB-D scene generator (host)
 
-The odometry kernels are compiled with the reference's numeric flags
+The odometry kernels (odo_*.cu) are compiled with the reference's numeric flags
 (--ftz=true --prec-div=false --prec-sqrt=false, src/CMakeLists.txt:116) so
 that projective association decisions round exactly as the reference's do.
 Translation units compile in parallel; a rebuild only happens when a source
@@ -30,7 +30,7 @@ NUMERIC = ["--ftz=true", "--prec-div=false", "--prec-sqrt=false"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
 
 # translation units of the tracker library
-CU_SOURCES = ["odo_maps.cu", "odo_track.cu", "odo_batch.cu", "cnn.cu"]
+CU_SOURCES = ["odo_maps.cu", "odo_track.cu", "odo_batch.cu", "cnn.cu", "synth_gpu.cu"]
 CPP_SOURCES = ["odo_host.cpp", "batch_host.cpp", "cnn_host.cpp"]
 
 
@@ -64,7 +64,9 @@ def build(force=False, verbose=False, extra_nvcc=()):
         objs.append(obj)
         if force or _newer(obj, [path, __file__] + headers):
             if src.endswith(".cu"):
-                cmd = [NVCC, *ARCH, *COMMON, *NUMERIC, "-Xcompiler", "-ffp-contract=off", *extra_nvcc, "-c", path,
+                # the reference's numeric flags for the tracking kernels only
+                numeric = NUMERIC if src.startswith("odo_") else []
+                cmd = [NVCC, *ARCH, *COMMON, *numeric, "-Xcompiler", "-ffp-contract=off", *extra_nvcc, "-c", path,
                        "-o", obj]
             else:
                 cmd = [NVCC, *COMMON, "-Xcompiler", "-ffp-contract=off", "-c", path, "-o", obj]
@@ -75,7 +77,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
     if force or jobs or _newer(LIB, objs):
         _run([NVCC, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs], verbose)
     synth_src = os.path.join(CSRC, "synth.cpp")
-    if force or _newer(SYNTH_LIB, [synth_src, __file__]):
+    if force or _newer(SYNTH_LIB, [synth_src, os.path.join(CSRC, "synth_common.h"), __file__]):
         _run(["g++", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c++17", "-ffp-contract=off",
               synth_src, "-o", SYNTH_LIB], verbose)
     return LIB

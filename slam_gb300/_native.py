@@ -62,7 +62,7 @@ class OdoStats(ctypes.Structure):
 class OdoPair(ctypes.Structure):
     _fields_ = [("width", c_int), ("height", c_int), ("fx", c_float), ("fy", c_float), ("cx", c_float),
                 ("cy", c_float), ("distThresh", c_float), ("angleThresh", c_float), ("depthCutoff", c_float),
-                ("levels", c_int), ("model_verts", c_void_p), ("model_norms", c_void_p), ("model_pitch", c_size_t),
+                ("levels", c_int), ("iterations", c_int * 3), ("model_verts", c_void_p), ("model_norms", c_void_p), ("model_pitch", c_size_t),
                 ("model_rgba", c_void_p), ("model_rgba_pitch", c_size_t), ("depth", c_void_p),
                 ("depth_pitch", c_size_t), ("rgba", c_void_p), ("rgba_pitch", c_size_t), ("prev_rgba", c_void_p),
                 ("prev_rgba_pitch", c_size_t), ("pose", c_float * 16)]
@@ -109,11 +109,29 @@ SIGNATURES = [
     ("odo_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
     ("odo_debug_profile", c_int, [c_void_p, P(c_double), c_int]),
     ("odo_debug_history", c_int, [c_void_p, P(c_double), c_int]),
+    ("odo_cnn_param_count", c_size_t, []),
+    ("odo_cnn_create", c_int, [c_int, P(c_void_p)]),
+    ("odo_cnn_destroy", c_int, [c_void_p]),
+    ("odo_cnn_set_stream", c_int, [c_void_p, c_void_p]),
+    ("odo_cnn_init_params", c_int, [c_void_p, ctypes.c_uint64]),
+    ("odo_cnn_set_params", c_int, [c_void_p, P(c_float)]),
+    ("odo_cnn_get_params", c_int, [c_void_p, P(c_float)]),
+    ("odo_cnn_set_loss_scale", c_int, [c_void_p, P(c_float)]),
+    ("odo_cnn_forward", c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    ("odo_cnn_train_step", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_float, P(c_float)]),
+    ("odo_cnn_pack_input", c_int, [c_void_p, P(OdoPair), c_int, c_void_p]),
+    ("odo_synth_render", c_int, [c_void_p, c_int, P(c_int), P(c_float), P(ctypes.c_uint64), c_int, c_int, c_int,
+                                 c_float, c_float, c_float, c_float, c_float, c_float, c_int, c_int, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("odo_cnn_gradients", c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_float), P(c_float)]),
+    ("odo_cnn_last_error", ctypes.c_char_p, [c_void_p]),
+    ("odo_cnn_debug_gemm", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),
     ("odo_batch_create", c_int, [c_int, P(c_void_p)]),
     ("odo_batch_destroy", c_int, [c_void_p]),
     ("odo_batch_set_stream", c_int, [c_void_p, c_void_p]),
     ("odo_batch_set_launch", c_int, [c_void_p, c_int, c_int]),
     ("odo_batch_track", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult)]),
+    ("odo_batch_track_init", c_int, [c_void_p, P(OdoPair), c_int, c_void_p, c_int, c_float, c_int, P(OdoPairResult)]),
     ("odo_batch_autotune", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult),
                                    P(c_int), P(c_int), P(c_float)]),
     ("odo_batch_last_error", ctypes.c_char_p, [c_void_p]),

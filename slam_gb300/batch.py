@@ -14,8 +14,10 @@ from .odometry import OdometryError, _check_cuda_tensor
 class FramePair:
     """Device inputs of one pair; `pose` is the model pose = starting pose."""
 
-    def __init__(self, cam, model_vert, model_norm, model_rgba, depth, rgba, prev_rgba, pose, levels=3):
+    def __init__(self, cam, model_vert, model_norm, model_rgba, depth, rgba, prev_rgba, pose, levels=3,
+                 iterations=(0, 0, 0)):
         self.cam, self.levels = cam, int(levels)
+        self.iterations = tuple(int(i) for i in iterations)
         self.model_vert, self.model_norm, self.model_rgba = model_vert, model_norm, model_rgba
         self.depth, self.rgba, self.prev_rgba = depth, rgba, prev_rgba
         self.pose = np.asarray(pose, np.float32).reshape(4, 4)
@@ -28,6 +30,8 @@ class FramePair:
         d.fx, d.fy, d.cx, d.cy = c.fx, c.fy, c.cx, c.cy
         d.distThresh = d.angleThresh = d.depthCutoff = 0.0
         d.levels = self.levels
+        for l in range(3):
+            d.iterations[l] = self.iterations[l]
         d.model_pitch = _check_cuda_tensor(self.model_vert, torch.float32, (4,), "model_vert")
         d.model_verts, d.model_norms = self.model_vert.data_ptr(), self.model_norm.data_ptr()
         d.model_rgba = self.model_rgba.data_ptr()
@@ -88,6 +92,21 @@ class BatchOdometry:
         res = (_native.OdoPairResult * len(pairs))()
         self._check(self._L.odo_batch_track(self._h, descs, len(pairs), int(bool(rgbOnly)), float(icpWeight),
                                             int(bool(fastOdom)), int(bool(so3)), res), "odo_batch_track")
+        return res
+
+    def track_init(self, pairs, init, rgbOnly=False, icpWeight=10.0, fastOdom=False, descs=None):
+        """Tracking from per-pair motion estimates: init is a CUDA float32
+        tensor [n, 6] (translation m, rotation vector rad of the live camera
+        in the model camera's frame); no SO3 stage."""
+        import torch
+        if not (isinstance(init, torch.Tensor) and init.is_cuda and init.dtype == torch.float32
+                and init.is_contiguous() and tuple(init.shape) == (len(pairs), 6)):
+            raise ValueError("init must be a contiguous CUDA float32 tensor [n, 6]")
+        descs = descs if descs is not None else self._descs(pairs)
+        res = (_native.OdoPairResult * len(pairs))()
+        self._check(self._L.odo_batch_track_init(self._h, descs, len(pairs), ctypes.c_void_p(init.data_ptr()),
+                                                 int(bool(rgbOnly)), float(icpWeight), int(bool(fastOdom)), res),
+                    "odo_batch_track_init")
         return res
 
     def autotune(self, pairs, rgbOnly=False, icpWeight=10.0, fastOdom=False, so3=True):

@@ -46,7 +46,7 @@ struct PairBufs {
 };
 
 using Layout = std::vector<std::tuple<int, int>>;
-using GKey = std::tuple<int, int, int, int, int, int, int, int>;
+using GKey = std::tuple<int, int, int, int, int, int, int, int, int>;
 
 }  // namespace
 
@@ -67,6 +67,7 @@ struct odo_batch {
     int threads = 256, ppt = 2;
     int max_nb[kLevels];
     int max_w = 0, max_h = 0;
+    float *init_dev = nullptr;  // [max_pairs][6] warm-start motions (odo_batch_track_init)
     std::map<GKey, cudaGraphExec_t> graphs;
     std::string last_error;
 };
@@ -319,7 +320,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             L.sobelScale = sobelScale;
             a.st = b->st_dev + i;
             a.ws = p.ws;
-            a.iters = (l < q.levels) ? base[l] : 0;
+            a.iters = (l < q.levels) ? (q.iterations[l] > 0 ? q.iterations[l] : base[l]) : 0;
             const int npx = L.cols * L.rows;
             a.nb_icp = a.iters ? blocks_for(b, npx) : 0;
             a.nb_rgb = a.iters ? (rgb ? a.nb_icp : 1) : 0;
@@ -346,7 +347,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
     }
 }
 
-cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, const int max_iters[kLevels]) {
+cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, const int max_iters[kLevels]) {
     cudaStream_t s = b->stream;
     cudaError_t e = cudaMemcpyAsync(b->args_dev, b->args_host, b->args_bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
@@ -366,6 +367,7 @@ cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, const int max
     if (e == cudaSuccess && rgb) e = launch_derivatives_batch((const DerivArgs *)A(b->o_deriv), n, W, Hh, s);
     if (e == cudaSuccess && so3) e = launch_so3_batch((const So3Args *)A(b->o_so3), n, s);
     if (e == cudaSuccess) e = launch_track_begin_batch(b->st_dev, n, s);
+    if (e == cudaSuccess && warm) e = launch_warm_seed_batch(b->st_dev, b->init_dev, n, s);
     for (int l = kLevels - 1; l >= 0 && e == cudaSuccess; --l)
         for (int j = 0; j < max_iters[l] && e == cudaSuccess; ++j)
             e = launch_level_iteration_batch((const PassArgs *)A(b->o_pass[l]), n, b->max_nb[l],
@@ -419,6 +421,7 @@ int odo_batch_create(int max_pairs, odo_batch_t **out) {
     if ((e = cudaMallocHost(&b->args_host, o)) != cudaSuccess) return bail(e, "cudaMallocHost(args)");
     std::memset(b->args_host, 0, o);
     if ((e = cudaMalloc(&b->st_dev, sizeof(TrackState) * np)) != cudaSuccess) return bail(e, "cudaMalloc(states)");
+    if ((e = cudaMalloc(&b->init_dev, sizeof(float) * 6 * np)) != cudaSuccess) return bail(e, "cudaMalloc(init)");
     if ((e = cudaMallocHost(&b->st_host, sizeof(TrackState) * np)) != cudaSuccess)
         return bail(e, "cudaMallocHost(states)");
     *out = b;
@@ -434,6 +437,7 @@ int odo_batch_destroy(odo_batch_t *b) {
     if (b->args_host) cudaFreeHost(b->args_host);
     if (b->st_dev) cudaFree(b->st_dev);
     if (b->st_host) cudaFreeHost(b->st_host);
+    if (b->init_dev) cudaFree(b->init_dev);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
     return ODO_OK;
@@ -459,8 +463,12 @@ int odo_batch_set_launch(odo_batch_t *b, int threads, int pixels_per_thread) {
     return ODO_OK;
 }
 
-int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
-                    int so3, odo_pair_result *results) {
+}  // extern "C"
+
+namespace {
+
+int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init, int rgbOnly, float icpWeight,
+               int fastOdom, int so3, odo_pair_result *results) {
     if (!b || !pairs || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
     for (int i = 0; i < npairs; ++i) {
         const odo_pair &q = pairs[i];
@@ -470,23 +478,29 @@ int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOn
             q.rgba_pitch < (size_t)q.width * 4 || q.model_rgba_pitch < (size_t)q.width * 4 || !(q.fx != 0) ||
             !(q.fy != 0))
             return ODO_ERR_ARG;
+        for (int l = 0; l < kLevels; ++l)
+            if (q.iterations[l] < 0 || q.iterations[l] > 20) return ODO_ERR_ARG;
     }
+    const int warm = init != nullptr;
+    if (warm) so3 = 0;
     int rc = ensure_layout(b, pairs, npairs);
     if (rc != ODO_OK) return rc;
     const int rgb = rgbOnly || icpWeight < 100;
     build_args(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3);
     int max_iters[kLevels] = {0, 0, 0};
-    int maxlev = 0;
-    for (int i = 0; i < npairs; ++i)
-        if (pairs[i].levels > maxlev) maxlev = pairs[i].levels;
     const int base[kLevels] = {fastOdom ? 3 : 10, 5, 4};
-    for (int l = 0; l < maxlev; ++l) max_iters[l] = base[l];
-    GKey key{npairs, rgb, so3 ? 1 : 0, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt};
+    for (int i = 0; i < npairs; ++i)
+        for (int l = 0; l < pairs[i].levels; ++l) {
+            const int it = pairs[i].iterations[l] > 0 ? pairs[i].iterations[l] : base[l];
+            if (it > max_iters[l]) max_iters[l] = it;
+        }
+    if (warm) BCK(cudaMemcpyAsync(b->init_dev, init, sizeof(float) * 6 * npairs, cudaMemcpyDeviceToDevice, b->stream));
+    GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt};
     auto it = b->graphs.find(key);
     if (it == b->graphs.end()) {
         cudaGraph_t g = nullptr;
         BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, max_iters);
+        cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters);
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
         if (e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -524,6 +538,21 @@ int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOn
         std::memcpy(r.lastb, st.lastb, sizeof(r.lastb));
     }
     return ODO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
+                    int so3, odo_pair_result *results) {
+    return track_impl(b, pairs, npairs, nullptr, rgbOnly, icpWeight, fastOdom, so3, results);
+}
+
+int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init_dev, int rgbOnly,
+                         float icpWeight, int fastOdom, odo_pair_result *results) {
+    if (!init_dev) return ODO_ERR_ARG;
+    return track_impl(b, pairs, npairs, init_dev, rgbOnly, icpWeight, fastOdom, 0, results);
 }
 
 int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,

@@ -1,0 +1,489 @@
+// Warm-start network kernels: forward, loss, backward and Adam, every
+// product on the tcgen05 tensor-core GEMM of umma_gemm.cuh (BF16 operands,
+// FP32 accumulation).  Layer l's GEMMs:
+//   forward      act[l+1][m][co] = relu(sum_k im2col(act[l])[m][k] W[co][k] + b[co])
+//   weight grad  dW[co][k]      = sum_m dpre[m][co] im2col(act[l])[m][k]     (split over m)
+//   data grad    dcol[m][k]     = sum_co dpre[m][co] W[co][k]
+//                dpre_prev      = col2im(dcol) * (act[l] > 0)
+// Rounding points (mirrored by the CPU oracle of this network): weights and
+// activations are BF16, the output and the loss gradient FP32 (rounded to
+// BF16 where they enter a product), dcol and all gradients FP32.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "cnn_internal.h"
+#include "umma_gemm.cuh"
+
+namespace slamgb {
+namespace cnn {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ uint16_t f2bf(float f) {
+    bf16 h = __float2bfloat16_rn(f);
+    return *reinterpret_cast<uint16_t *>(&h);
+}
+__device__ __forceinline__ float bf2f(uint16_t u) { return __uint_as_float((uint32_t)u << 16); }
+__device__ __forceinline__ uint16_t h2bf(uint16_t h) {
+    __half x = *reinterpret_cast<__half *>(&h);
+    return f2bf(__half2float(x));
+}
+__device__ __forceinline__ uint4 pack8(const uint16_t (&v)[8]) {
+    uint4 r;
+    r.x = v[0] | ((uint32_t)v[1] << 16);
+    r.y = v[2] | ((uint32_t)v[3] << 16);
+    r.z = v[4] | ((uint32_t)v[5] << 16);
+    r.w = v[6] | ((uint32_t)v[7] << 16);
+    return r;
+}
+__device__ __forceinline__ uint4 zero4() { return make_uint4(0, 0, 0, 0); }
+
+// ---------------------------------------------------------------- loaders
+// Row-major BF16 [rows][ld], K columns used (ld % 8 == 0, 16-byte aligned base).
+struct LdDense {
+    const uint16_t *p;
+    int rows, K, ld;
+    __device__ uint4 operator()(int r, int k8) const {
+        const int k = k8 * 8;
+        if (r >= rows || k >= K) return zero4();
+        if (k + 8 <= K) return __ldg(reinterpret_cast<const uint4 *>(p + (size_t)r * ld + k));
+        uint16_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = (k + j < K) ? p[(size_t)r * ld + k + j] : 0;
+        return pack8(v);
+    }
+};
+// Row-major FP32 [rows][ld] rounded to BF16.
+struct LdDenseF32 {
+    const float *p;
+    int rows, K, ld;
+    __device__ uint4 operator()(int r, int k8) const {
+        uint16_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = k8 * 8 + j;
+            v[j] = (r < rows && k < K) ? f2bf(p[(size_t)r * ld + k]) : 0;
+        }
+        return pack8(v);
+    }
+};
+// Transposed view of a row-major BF16 matrix G[K][ld]: A(r, k) = G[k][r].
+struct LdTrans {
+    const uint16_t *p;
+    int rows, K, ld;
+    __device__ uint4 operator()(int r, int k8) const {
+        uint16_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = k8 * 8 + j;
+            v[j] = (r < rows && k < K) ? p[(size_t)k * ld + r] : 0;
+        }
+        return pack8(v);
+    }
+};
+struct LdTransF32 {
+    const float *p;
+    int rows, K, ld;
+    __device__ uint4 operator()(int r, int k8) const {
+        uint16_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = k8 * 8 + j;
+            v[j] = (r < rows && k < K) ? f2bf(p[(size_t)k * ld + r]) : 0;
+        }
+        return pack8(v);
+    }
+};
+
+// Geometry of one 3x3 / stride 2 / pad 1 convolution over NHWC input.
+struct ConvGeo {
+    int B, H, W, C, Ho, Wo;
+    __device__ int M() const { return B * Ho * Wo; }
+    // input element index of im2col(m, k), or -1 for padding
+    __device__ long long src(int m, int k) const {
+        const int tap = k / C, ci = k - tap * C;
+        const int ky = tap / 3, kx = tap - 3 * ky;
+        const int ox = m % Wo;
+        const int t = m / Wo;
+        const int oy = t % Ho, b = t / Ho;
+        const int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;
+        if (iy < 0 || iy >= H || ix < 0 || ix >= W) return -1;
+        return (((long long)b * H + iy) * W + ix) * C + ci;
+    }
+};
+// Implicit im2col A(m, k) of a BF16 (or FP16 when F16) NHWC input; C % 8 == 0
+// so the 8 values of a K group share one tap.
+template <bool F16>
+struct LdIm2col {
+    const uint16_t *x;
+    ConvGeo g;
+    __device__ uint4 operator()(int m, int k8) const {
+        const int k = k8 * 8;
+        if (m >= g.M() || k >= 9 * g.C) return zero4();
+        const long long o = g.src(m, k);
+        if (o < 0) return zero4();
+        uint4 v = __ldg(reinterpret_cast<const uint4 *>(x + o));
+        if (!F16) return v;
+        const uint16_t *h = reinterpret_cast<const uint16_t *>(&v);
+        uint16_t b[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) b[j] = h2bf(h[j]);
+        return pack8(b);
+    }
+};
+// Transposed im2col: B(k, m) = im2col(m, k) for 8 consecutive positions m.
+template <bool F16>
+struct LdIm2colT {
+    const uint16_t *x;
+    ConvGeo g;
+    __device__ uint4 operator()(int k, int m8) const {
+        uint16_t v[8];
+        const int M = g.M();
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int m = m8 * 8 + j;
+            uint16_t u = 0;
+            if (k < 9 * g.C && m < M) {
+                const long long o = g.src(m, k);
+                if (o >= 0) u = F16 ? h2bf(x[o]) : x[o];
+            }
+            v[j] = u;
+        }
+        return pack8(v);
+    }
+};
+
+// -------------------------------------------------------------- epilogues
+struct EpBiasAct {  // y = act(v + bias) as BF16
+    uint16_t *y;
+    const float *bias;
+    int N, ld, relu;
+    __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = n0 + j;
+            if (n < N) {
+                float f = v[j] + bias[n];
+                if (relu) f = fmaxf(f, 0.f);
+                y[(size_t)m * ld + n] = f2bf(f);
+            }
+        }
+    }
+};
+struct EpBiasF32 {
+    float *y;
+    const float *bias;
+    int N, ld;
+    __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (n0 + j < N) y[(size_t)m * ld + n0 + j] = v[j] + bias[n0 + j];
+    }
+};
+struct EpStore {
+    float *y;
+    int N, ld;
+    __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (n0 + j < N) y[(size_t)m * ld + n0 + j] = v[j];
+    }
+};
+struct EpAtomic {
+    float *y;
+    int N, ld;
+    __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (n0 + j < N) atomicAdd(&y[(size_t)m * ld + n0 + j], v[j]);
+    }
+};
+struct EpMask {  // dst = BF16(v) where the activation is positive, else 0
+    uint16_t *dst;
+    const uint16_t *act;
+    int N, ld;
+    __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = n0 + j;
+            if (n < N) {
+                const size_t o = (size_t)m * ld + n;
+                dst[o] = bf2f(act[o]) > 0.f ? f2bf(v[j]) : (uint16_t)0;
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_col2im_mask(const float *dcol, const uint16_t *act, uint16_t *dpre, int B, int H, int W, int C,
+                              int Ho, int Wo) {
+    const long long n = (long long)B * H * W * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(i % C);
+        long long t = i / C;
+        const int ix = (int)(t % W);
+        t /= W;
+        const int iy = (int)(t % H);
+        const int b = (int)(t / H);
+        float s = 0.f;
+        for (int ky = 0; ky < 3; ++ky) {
+            const int ty = iy + 1 - ky;
+            if (ty < 0 || (ty & 1)) continue;
+            const int oy = ty >> 1;
+            if (oy >= Ho) continue;
+            for (int kx = 0; kx < 3; ++kx) {
+                const int tx = ix + 1 - kx;
+                if (tx < 0 || (tx & 1)) continue;
+                const int ox = tx >> 1;
+                if (ox >= Wo) continue;
+                s += dcol[(((long long)b * Ho + oy) * Wo + ox) * 9 * C + (ky * 3 + kx) * C + ci];
+            }
+        }
+        dpre[i] = bf2f(act[i]) > 0.f ? f2bf(s) : (uint16_t)0;
+    }
+}
+
+// db[n] += sum over rows m of g[m][n] (BF16 or FP32 rows of length ld)
+template <typename T>
+__global__ void k_colsum(const T *g, int M, int N, int ld, float *db) {
+    __shared__ float sm[8][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int n = blockIdx.x * 32 + tx;
+    float s = 0.f;
+    if (n < N)
+        for (int m = blockIdx.y * 8 + ty; m < M; m += gridDim.y * 8) {
+            if constexpr (sizeof(T) == 2) s += bf2f(g[(size_t)m * ld + n]);  // BF16 bits
+            else s += g[(size_t)m * ld + n];
+        }
+    sm[ty][tx] = s;
+    __syncthreads();
+    if (ty == 0 && n < N) {
+        float t = 0.f;
+        for (int k = 0; k < 8; ++k) t += sm[k][tx];
+        atomicAdd(&db[n], t);
+    }
+}
+
+// loss = mean_b sum_i (s_i (out - label))^2 ; dout = d loss / d out
+__global__ void k_loss(const float *out, const float *label, const float *scale, int B, float *dout, float *loss) {
+    __shared__ float red[256];
+    float acc = 0.f;
+    for (int i = threadIdx.x; i < B * kOut; i += blockDim.x) {
+        const float s = scale[i % kOut];
+        const float d = out[i] - label[i];
+        acc += s * s * d * d;
+        dout[i] = 2.f * s * s * d / (float)B;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *loss = red[0] / (float)B;
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+__global__ void k_to_bf16(const float *p, uint16_t *q, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        q[i] = f2bf(p[i]);
+}
+// wt[c][r] = w[r][c] (BF16), rows padded with zeros up to ldt
+__global__ void k_transpose_bf16(const uint16_t *w, int rows, int cols, uint16_t *wt, int ldt) {
+    const long long n = (long long)cols * ldt;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i / ldt), r = (int)(i % ldt);
+        wt[i] = r < rows ? w[(size_t)r * cols + c] : (uint16_t)0;
+    }
+}
+
+// Network input of pair blockIdx.z: s x s block means of the valid depths
+// (metres; 0 where no pixel is valid) and of the intensities (the tracker's
+// weighting of the RGBA bytes, 0..1), FP16, four zero channels.
+__global__ void k_pack(const PackArgs *args, uint16_t *out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= kInW || y >= kInH) return;
+    const PackArgs a = args[blockIdx.z];
+    float md = 0.f, mg = 0.f, ld = 0.f, lg = 0.f;
+    int nm = 0, nl = 0;
+    for (int dy = 0; dy < a.s; ++dy) {
+        const int yy = y * a.s + dy;
+        const float4 *mv = reinterpret_cast<const float4 *>(reinterpret_cast<const char *>(a.model_verts) +
+                                                            (size_t)yy * a.model_pitch);
+        const uchar4 *mc = reinterpret_cast<const uchar4 *>(a.model_rgba + (size_t)yy * a.model_rgba_pitch);
+        const uint16_t *dd = reinterpret_cast<const uint16_t *>(reinterpret_cast<const char *>(a.depth) +
+                                                                (size_t)yy * a.depth_pitch);
+        const uchar4 *lc = reinterpret_cast<const uchar4 *>(a.rgba + (size_t)yy * a.rgba_pitch);
+        for (int dx = 0; dx < a.s; ++dx) {
+            const int xx = x * a.s + dx;
+            const float z = mv[xx].z;
+            if (z > 0.f) {
+                md += z;
+                ++nm;
+            }
+            const uchar4 c = mc[xx];
+            mg += (float)c.x * 0.114f + (float)c.y * 0.299f + (float)c.z * 0.587f;
+            const uint16_t d = dd[xx];
+            if (d) {
+                ld += (float)d * 1e-3f;
+                ++nl;
+            }
+            const uchar4 e = lc[xx];
+            lg += (float)e.x * 0.114f + (float)e.y * 0.299f + (float)e.z * 0.587f;
+        }
+    }
+    const float inv = 1.f / (255.f * a.s * a.s);
+    __align__(16) __half h[8];
+    h[0] = __float2half_rn(nm ? md / nm : 0.f);
+    h[1] = __float2half_rn(mg * inv);
+    h[2] = __float2half_rn(nl ? ld / nl : 0.f);
+    h[3] = __float2half_rn(lg * inv);
+    h[4] = h[5] = h[6] = h[7] = __float2half_rn(0.f);
+    uint16_t *o = out + (((size_t)blockIdx.z * kInH + y) * kInW + x) * kInC;
+    *reinterpret_cast<uint4 *>(o) = *reinterpret_cast<const uint4 *>(h);
+}
+
+int grid_for(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    if (b > 152 * 16) b = 152 * 16;
+    return (int)(b < 1 ? 1 : b);
+}
+
+// Conv layer l geometry for batch B.
+ConvGeo conv_geo(int l, int B) { return ConvGeo{B, kH[l], kW[l], kCin[l], kH[l + 1], kW[l + 1]}; }
+
+template <class LA, class LB, class EP>
+cudaError_t gemm(const LA &a, const LB &b, const EP &e, int M, int N, int K, int splits, int *err, cudaStream_t s) {
+    if (N <= 32) return launch_umma_gemm<32>(a, b, e, M, N, K, splits, 0, err, s);
+    if (N <= 64) return launch_umma_gemm<64>(a, b, e, M, N, K, splits, 0, err, s);
+    return launch_umma_gemm<128>(a, b, e, M, N, K, splits, 0, err, s);
+}
+
+}  // namespace
+
+#define CNN_CK(x)                              \
+    do {                                       \
+        cudaError_t e_ = (x);                  \
+        if (e_ != cudaSuccess) return e_;      \
+    } while (0)
+
+cudaError_t cnn_forward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
+    const ParamLayout &P = n.L;
+    for (int l = 0; l < kConv; ++l) {
+        const ConvGeo g = conv_geo(l, B);
+        const int M = B * g.Ho * g.Wo, N = kCout[l], K = 9 * kCin[l];
+        const LdDense wb{n.wbf + P.w[l], N, K, K};
+        const EpBiasAct ep{n.act[l + 1], n.master + P.b[l], N, N, 1};
+        if (l == 0) CNN_CK(gemm(LdIm2col<true>{input, g}, wb, ep, M, N, K, 1, n.err, s));
+        else CNN_CK(gemm(LdIm2col<false>{n.act[l], g}, wb, ep, M, N, K, 1, n.err, s));
+    }
+    const int l1 = kConv, l2 = kConv + 1;
+    CNN_CK(gemm(LdDense{n.act[kConv], B, kFlat, kFlat}, LdDense{n.wbf + P.w[l1], kHidden, kFlat, kFlat},
+                EpBiasAct{n.hid, n.master + P.b[l1], kHidden, kHidden, 1}, B, kHidden, kFlat, 1, n.err, s));
+    CNN_CK(gemm(LdDense{n.hid, B, kHidden, kHidden}, LdDense{n.wbf + P.w[l2], kOut, kHidden, kHidden},
+                EpBiasF32{n.out, n.master + P.b[l2], kOut, kOut}, B, kOut, kHidden, 1, n.err, s));
+    return cudaSuccess;
+}
+
+cudaError_t cnn_pack(const PackArgs *args_dev, int n, uint16_t *out, cudaStream_t s) {
+    dim3 blk(32, 8), grid((kInW + 31) / 32, (kInH + 7) / 8, n);
+    k_pack<<<grid, blk, 0, s>>>(args_dev, out);
+    return cudaGetLastError();
+}
+
+cudaError_t cnn_loss(Net &n, const float *labels, int B, cudaStream_t s) {
+    k_loss<<<1, 256, 0, s>>>(n.out, labels, n.scale, B, n.dout, n.loss);
+    return cudaGetLastError();
+}
+
+cudaError_t cnn_backward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
+    const ParamLayout &P = n.L;
+    CNN_CK(cudaMemsetAsync(n.grad, 0, P.total * sizeof(float), s));
+    const int l1 = kConv, l2 = kConv + 1;
+    // fc2
+    CNN_CK(gemm(LdTransF32{n.dout, kOut, B, kOut}, LdTrans{n.hid, kHidden, B, kHidden},
+                EpStore{n.grad + P.w[l2], kHidden, kHidden}, kOut, kHidden, B, 1, n.err, s));
+    k_colsum<float><<<dim3(1, 8), 256, 0, s>>>(n.dout, B, kOut, kOut, n.grad + P.b[l2]);
+    CNN_CK(gemm(LdDenseF32{n.dout, B, kOut, kOut}, LdDense{n.wt + P.wt[l2], kHidden, kOut, P.wt_ld[l2]},
+                EpMask{n.dpre_hid, n.hid, kHidden, kHidden}, B, kHidden, kOut, 1, n.err, s));
+    // fc1
+    CNN_CK(gemm(LdTrans{n.dpre_hid, kHidden, B, kHidden}, LdTrans{n.act[kConv], kFlat, B, kFlat},
+                EpStore{n.grad + P.w[l1], kFlat, kFlat}, kHidden, kFlat, B, 1, n.err, s));
+    k_colsum<uint16_t><<<dim3((kHidden + 31) / 32, 8), 256, 0, s>>>(n.dpre_hid, B, kHidden, kHidden, n.grad + P.b[l1]);
+    CNN_CK(gemm(LdDense{n.dpre_hid, B, kHidden, kHidden}, LdDense{n.wt + P.wt[l1], kFlat, kHidden, P.wt_ld[l1]},
+                EpMask{n.dpre[kConv], n.act[kConv], kFlat, kFlat}, B, kFlat, kHidden, 1, n.err, s));
+    CNN_CK(cudaGetLastError());
+    // conv layers, last to first
+    for (int l = kConv - 1; l >= 0; --l) {
+        const ConvGeo g = conv_geo(l, B);
+        const int Mpos = B * g.Ho * g.Wo, Co = kCout[l], K = 9 * kCin[l];
+        const uint16_t *dp = n.dpre[l + 1];
+        // weight gradient, split over positions
+        const int kchunks = (Mpos + kGemmKChunk - 1) / kGemmKChunk;
+        const int tiles = (K + 127) / 128;
+        int splits = 2 * 152 / tiles;
+        if (splits > kchunks) splits = kchunks;
+        if (splits < 1) splits = 1;
+        const LdTrans da{dp, Co, Mpos, Co};
+        const EpAtomic ew{n.grad + P.w[l], K, K};
+        if (l == 0) CNN_CK(launch_umma_gemm<128>(da, LdIm2colT<true>{input, g}, ew, Co, K, Mpos, splits, 0, n.err, s));
+        else CNN_CK(launch_umma_gemm<128>(da, LdIm2colT<false>{n.act[l], g}, ew, Co, K, Mpos, splits, 0, n.err, s));
+        k_colsum<uint16_t><<<dim3((Co + 31) / 32, 64), 256, 0, s>>>(dp, Mpos, Co, Co, n.grad + P.b[l]);
+        CNN_CK(cudaGetLastError());
+        if (l == 0) break;
+        // data gradient
+        CNN_CK(gemm(LdDense{dp, Mpos, Co, Co}, LdDense{n.wt + P.wt[l], K, Co, P.wt_ld[l]}, EpStore{n.dcol, K, K},
+                    Mpos, K, Co, 1, n.err, s));
+        const long long ne = (long long)B * g.H * g.W * g.C;
+        k_col2im_mask<<<grid_for(ne, 256), 256, 0, s>>>(n.dcol, n.act[l], n.dpre[l], B, g.H, g.W, g.C, g.Ho, g.Wo);
+        CNN_CK(cudaGetLastError());
+    }
+    return cudaSuccess;
+}
+
+cudaError_t cnn_adam(Net &n, float lr, float beta1, float beta2, float eps, cudaStream_t s) {
+    n.step += 1;
+    const float c1 = 1.f - powf(beta1, (float)n.step), c2 = 1.f - powf(beta2, (float)n.step);
+    k_adam<<<grid_for((long long)n.L.total, 256), 256, 0, s>>>(n.master, n.grad, n.adam_m, n.adam_v, n.L.total, lr,
+                                                                 beta1, beta2, eps, c1, c2);
+    CNN_CK(cudaGetLastError());
+    return cnn_refresh_weights(n, s);
+}
+
+cudaError_t cnn_refresh_weights(Net &n, cudaStream_t s) {
+    k_to_bf16<<<grid_for((long long)n.L.total, 256), 256, 0, s>>>(n.master, n.wbf, n.L.total);
+    CNN_CK(cudaGetLastError());
+    for (int l = 0; l < kLayers; ++l) {
+        const long long ne = (long long)w_cols(l) * n.L.wt_ld[l];
+        k_transpose_bf16<<<grid_for(ne, 256), 256, 0, s>>>(n.wbf + n.L.w[l], w_rows(l), w_cols(l), n.wt + n.L.wt[l],
+                                                          n.L.wt_ld[l]);
+        CNN_CK(cudaGetLastError());
+    }
+    return cudaSuccess;
+}
+
+cudaError_t cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M, int N, int K, int bn, int layout,
+                           int *err, cudaStream_t s) {
+    const LdDense la{A, M, K, (K + 7) & ~7}, lb{B, N, K, (K + 7) & ~7};
+    const EpStore ep{C, N, N};
+    if (bn == 32) return launch_umma_gemm<32>(la, lb, ep, M, N, K, 1, layout, err, s);
+    if (bn == 64) return launch_umma_gemm<64>(la, lb, ep, M, N, K, 1, layout, err, s);
+    if (bn == 128) return launch_umma_gemm<128>(la, lb, ep, M, N, K, 1, layout, err, s);
+    if (bn == 256) return launch_umma_gemm<256>(la, lb, ep, M, N, K, 1, layout, err, s);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace cnn
+}  // namespace slamgb

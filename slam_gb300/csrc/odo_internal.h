@@ -216,6 +216,7 @@ KMats make_kmats(const Intr &K);
 // thread-block cluster per pair for SO3); `states` is a device array
 cudaError_t launch_track_begin_batch(TrackState *states, int npairs, cudaStream_t s);
 cudaError_t launch_stamp_batch(TrackState *states, int npairs, cudaStream_t s);
+cudaError_t launch_warm_seed_batch(TrackState *states, const float *init, int npairs, cudaStream_t s);
 cudaError_t launch_track_end_batch(TrackState *states, int npairs, cudaStream_t s);
 cudaError_t launch_so3_batch(const So3Args *args, int npairs, cudaStream_t s);
 cudaError_t launch_level_iteration_batch(const PassArgs *args, int npairs, int max_nb_icp, int max_nb_rgb,

@@ -11,37 +11,18 @@
 #include <cstring>
 #include <algorithm>
 
+#include "synth_common.h"
+
 namespace {
 
-inline uint64_t splitmix64(uint64_t x) {
-    x += 0x9E3779B97F4A7C15ull;
-    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-    return x ^ (x >> 31);
-}
-inline double u01(uint64_t h) { return (double)(h >> 11) * (1.0 / 9007199254740992.0); }
-
-struct Rng {
-    uint64_t s;
-    explicit Rng(uint64_t seed) : s(splitmix64(seed ^ 0x5eed5eedull)) {}
-    double uni() { s = splitmix64(s); return u01(s); }
-    double uni(double a, double b) { return a + (b - a) * uni(); }
-};
+using synth::Rng;
+using synth::splitmix64;
+using synth::u01;
 
 // Improved Perlin gradient noise (Perlin 2002) with a seeded permutation.
 struct Perlin {
     int p[512];
-    explicit Perlin(uint64_t seed) {
-        int q[256];
-        for (int i = 0; i < 256; ++i) q[i] = i;
-        Rng r(seed);
-        for (int i = 255; i > 0; --i) {
-            int j = (int)(r.uni() * (i + 1));
-            if (j > i) j = i;
-            std::swap(q[i], q[j]);
-        }
-        for (int i = 0; i < 512; ++i) p[i] = q[i & 255];
-    }
+    explicit Perlin(uint64_t seed) { synth::perlin_perm(seed, p); }
     static double fade(double t) { return t * t * t * (t * (t * 6 - 15) + 10); }
     static double lerp(double t, double a, double b) { return a + t * (b - a); }
     static double grad(int h, double x, double y, double z) {
@@ -66,19 +47,6 @@ struct Perlin {
 }  // namespace
 
 extern "C" {
-
-#define SYNTH_MAX_SPH 128
-
-typedef struct {
-    float bmin[3], bmax[3];   // interior of the box (metres, world frame)
-    int nsph;
-    float sph[SYNTH_MAX_SPH][4];     // centre xyz, radius
-    float sph_col[SYNTH_MAX_SPH][3]; // base colour 0..1
-    float wall_col[6][3];
-    float tex_freq;   // texture cycles per metre
-    float tex_amp;    // 0..1 texture contrast
-    uint64_t tex_seed;
-} synth_scene;
 
 // A 6x4x3 m box room (x in [-3,3], y in [-1.5,1.5] (y down), z in [-2,2])
 // with `nspheres` spheres of radius U(0.1, 0.5) kept clear of a 0.8 m ball

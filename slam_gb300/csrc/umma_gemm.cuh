@@ -1,0 +1,146 @@
+// Generic BF16 tensor-core GEMM on tcgen05:  C[m, n] = sum_k A(m, k) B(n, k)
+// with FP32 accumulation in TMEM.
+//
+// A CTA of 128 threads owns a 128 x BN output tile.  K is consumed in chunks
+// of 64: all threads stage the chunk's A (128 x 64) and B (BN x 64) tiles into
+// shared memory through the loader functors (which implement implicit
+// im2col, transposes and zero padding; each returns 8 bf16 of one row), one
+// thread issues four K = 16 MMAs and commits them to the stage's mbarrier,
+// and the next chunk is staged into the other buffer while they run.  The
+// epilogue reads the accumulator from TMEM (warp w: rows 32 w .. 32 w + 31)
+// and hands 8 consecutive columns of a row at a time to the epilogue functor.
+// gridDim.z > 1 splits K (the epilogue then accumulates, e.g. atomically).
+//
+// Loader:   __device__ uint4 operator()(int row, int k8) const   (k = 8 k8 .. 8 k8 + 7)
+// Epilogue: __device__ void operator()(int m, int n0, const float (&v)[8]) const
+#pragma once
+#include <cstdint>
+
+#include "umma.cuh"
+
+namespace slamgb {
+
+constexpr int kGemmThreads = 128;
+constexpr int kGemmKChunk = 64;
+constexpr uint32_t kGemmWaitPolls = 1u << 22;
+
+template <int BN>
+constexpr int gemm_smem_bytes() {
+    return 2 * (128 * kGemmKChunk * 2 + BN * kGemmKChunk * 2) + 1024;
+}
+
+// `layout` selects the operand core-matrix offsets (0: K-direction 128 B,
+// row-direction 1024 B; 1: the two exchanged) for the layout self-check.
+template <int BN, class LA, class LB, class EP>
+__global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep, int M, int N, int kchunks,
+                                                            int chunks_per_split, int layout, int *err) {
+    static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "BN");
+    constexpr int A_BYTES = 128 * kGemmKChunk * 2, B_BYTES = BN * kGemmKChunk * 2, STAGE = A_BYTES + B_BYTES;
+    constexpr uint32_t IDESC = umma::idesc_bf16_f32(128, BN);
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+    const int c_begin = blockIdx.z * chunks_per_split;
+    const int c_end = min(kchunks, c_begin + chunks_per_split);
+    const int nch = c_end - c_begin;
+    if (nch <= 0) return;
+    if (warp == 0) {
+        umma::tmem_alloc(&tmem_base, BN < 32 ? 32 : BN);
+        umma::tmem_relinquish();
+    }
+    if (tid == 0) {
+        umma::mbar_init(&mbar[0], 1);
+        umma::mbar_init(&mbar[1], 1);
+        umma::mbar_fence_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const uint32_t lbo = layout ? 1024u : 128u, sbo = layout ? 128u : 1024u;
+    bool ok = true;
+    int c = 0;
+    for (; c < nch; ++c) {
+        const int s = c & 1;
+        uint8_t *sa = smem + s * STAGE;
+        uint8_t *sb = sa + A_BYTES;
+        // the MMAs of chunk c - 2 read this stage; the decision to go on is
+        // block-uniform so every thread leaves the loop at the same chunk
+        if (c >= 2) {
+            ok = umma::mbar_wait(&mbar[s], ((c - 2) >> 1) & 1, kGemmWaitPolls);
+            if (!__syncthreads_and(ok)) break;
+        }
+        const int k8_0 = (c_begin + c) * (kGemmKChunk / 8);
+        // thread i writes bytes [16 i, 16 i + 16): row group i >> 6, K group
+        // (i >> 3) & 7, row (i & 7) -- conflict-free 16-byte stores
+#pragma unroll 4
+        for (int i = tid; i < 128 * 8; i += kGemmThreads) {
+            const int row = ((i >> 6) << 3) + (i & 7), kg = (i >> 3) & 7;
+            *reinterpret_cast<uint4 *>(sa + i * 16) = la(m0 + row, k8_0 + kg);
+        }
+#pragma unroll 4
+        for (int i = tid; i < BN * 8; i += kGemmThreads) {
+            const int row = ((i >> 6) << 3) + (i & 7), kg = (i >> 3) & 7;
+            *reinterpret_cast<uint4 *>(sb + i * 16) = lb(n0 + row, k8_0 + kg);
+        }
+        umma::fence_smem_to_async();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            const uint32_t a0 = umma::smem_u32(sa), b0 = umma::smem_u32(sb);
+#pragma unroll
+            for (int k = 0; k < kGemmKChunk / 16; ++k)
+                umma::mma_bf16(tmem, umma::smem_desc(a0 + k * 256, lbo, sbo), umma::smem_desc(b0 + k * 256, lbo, sbo),
+                               IDESC, (c > 0 || k > 0) ? 1u : 0u);
+            umma::mma_commit(&mbar[s]);
+        }
+    }
+    // all MMAs issued so far are done when the last commit's phase completes
+    const int last = c - 1;
+    ok = ok && umma::mbar_wait(&mbar[last & 1], (last >> 1) & 1, kGemmWaitPolls);
+    ok = __syncthreads_and(ok) && c == nch;
+    umma::fence_after_sync();
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int j = 0; j < BN; j += 8) {
+            float v[8];
+            umma::tmem_ld8(trow + j, v);
+            if (row < M && n0 + j < N) ep(row, n0 + j, v);
+        }
+    } else if (tid == 0 && err) {
+        atomicExch(err, 1);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, BN < 32 ? 32 : BN);
+}
+
+// Host-side launch helper (in a .cu translation unit).
+template <int BN, class LA, class LB, class EP>
+cudaError_t launch_umma_gemm(const LA &la, const LB &lb, const EP &ep, int M, int N, int K, int splits, int layout,
+                             int *err, cudaStream_t s) {
+    if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+    const int kchunks = (K + kGemmKChunk - 1) / kGemmKChunk;
+    if (splits < 1) splits = 1;
+    if (splits > kchunks) splits = kchunks;
+    const int per = (kchunks + splits - 1) / splits;
+    splits = (kchunks + per - 1) / per;
+    constexpr int smem = gemm_smem_bytes<BN>();
+    static bool attr_set = false;  // per instantiation
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN, LA, LB, EP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dim3 grid((M + 127) / 128, (N + BN - 1) / BN, splits);
+    k_umma_gemm<BN, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, per, layout, err);
+    return cudaGetLastError();
+}
+
+}  // namespace slamgb

@@ -1,0 +1,287 @@
+"""Learned warm start of the tracker (C ABI odo_cnn_*; no counterpart in the
+reference).
+
+A BF16 CNN proposes the SE(3) motion of a frame pair from both frames'
+160x120 depth and gray images; its forward and backward products run on the
+library's tcgen05 GEMM.  Inputs are CUDA tensors: [B, 120, 160, 8] float16
+(model depth m, model gray, live depth m, live gray, four zeros); outputs
+[B, 6] float32 (translation m, rotation vector rad).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .odometry import OdometryError
+
+IN_H, IN_W, IN_C = 120, 160, 8
+DEFAULT_LOSS_SCALE = (10.0, 10.0, 10.0, 6.0, 6.0, 6.0)
+
+
+class WarmStartNet:
+    def __init__(self, max_batch=256, seed=1, stream=None):
+        self._L = _native.load()
+        h = ctypes.c_void_p()
+        rc = self._L.odo_cnn_create(int(max_batch), ctypes.byref(h))
+        if rc != 0:
+            raise OdometryError(rc, "odo_cnn_create failed (%s)" % self._L.odo_status_string(rc).decode())
+        self._h = h
+        self.max_batch = int(max_batch)
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+        self._check(self._L.odo_cnn_set_stream(self._h, ctypes.c_void_p(stream)), "odo_cnn_set_stream")
+        if seed != 1:
+            self._check(self._L.odo_cnn_init_params(self._h, ctypes.c_uint64(seed)), "odo_cnn_init_params")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise OdometryError(rc, "%s: %s %s" % (what, self._L.odo_status_string(rc).decode(),
+                                                   self._L.odo_cnn_last_error(self._h).decode()))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.odo_cnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def param_count():
+        return int(_native.load().odo_cnn_param_count())
+
+    def get_params(self):
+        p = np.zeros(self.param_count(), np.float32)
+        self._check(self._L.odo_cnn_get_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                    "odo_cnn_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32).reshape(-1)
+        if p.size != self.param_count():
+            raise ValueError("expected %d parameters" % self.param_count())
+        self._check(self._L.odo_cnn_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                    "odo_cnn_set_params")
+
+    def set_loss_scale(self, scale):
+        s = np.ascontiguousarray(scale, np.float32).reshape(6)
+        self._check(self._L.odo_cnn_set_loss_scale(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                    "odo_cnn_set_loss_scale")
+
+    def _inp(self, x):
+        import torch
+        if not (isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == torch.float16 and x.is_contiguous()
+                and x.dim() == 4 and tuple(x.shape[1:]) == (IN_H, IN_W, IN_C)):
+            raise ValueError("input must be a contiguous CUDA float16 tensor [B, 120, 160, 8]")
+        if not 1 <= x.shape[0] <= self.max_batch:
+            raise ValueError("batch must be in 1..%d" % self.max_batch)
+        return x.shape[0]
+
+    def pack(self, frame_pairs, out):
+        """Network inputs of FramePairs (level-0 size (160 s) x (120 s)) into
+        out[:len(frame_pairs)] (CUDA float16 [>= n, 120, 160, 8])."""
+        import torch
+        n = len(frame_pairs)
+        if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float16 and out.is_contiguous()
+                and out.dim() == 4 and tuple(out.shape[1:]) == (IN_H, IN_W, IN_C) and out.shape[0] >= n):
+            raise ValueError("out must be a contiguous CUDA float16 tensor [>=n, 120, 160, 8]")
+        arr = (_native.OdoPair * n)()
+        for i, p in enumerate(frame_pairs):
+            arr[i] = p.desc()
+        self._check(self._L.odo_cnn_pack_input(self._h, arr, n, ctypes.c_void_p(out.data_ptr())),
+                    "odo_cnn_pack_input")
+        return out
+
+    def forward(self, x, out=None):
+        import torch
+        B = self._inp(x)
+        if out is None:
+            out = torch.empty((B, 6), dtype=torch.float32, device=x.device)
+        self._check(self._L.odo_cnn_forward(self._h, ctypes.c_void_p(x.data_ptr()), B, ctypes.c_void_p(out.data_ptr())),
+                    "odo_cnn_forward")
+        return out
+
+    def train_step(self, x, labels, lr, want_loss=True):
+        B = self._inp(x)
+        loss = ctypes.c_float()
+        self._check(self._L.odo_cnn_train_step(self._h, ctypes.c_void_p(x.data_ptr()),
+                                               ctypes.c_void_p(labels.data_ptr()), B, float(lr),
+                                               ctypes.byref(loss) if want_loss else None), "odo_cnn_train_step")
+        return loss.value if want_loss else None
+
+    def gradients(self, x, labels):
+        B = self._inp(x)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_float()
+        self._check(self._L.odo_cnn_gradients(self._h, ctypes.c_void_p(x.data_ptr()),
+                                              ctypes.c_void_p(labels.data_ptr()), B,
+                                              g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss)),
+                    "odo_cnn_gradients")
+        return g, loss.value
+
+
+def debug_gemm(A, B, bn=128, layout=0):
+    """C = A B^T on the library's tensor-core GEMM (A [M, K], B [N, K] bf16
+    CUDA tensors, K a multiple of 8)."""
+    import torch
+    L = _native.load()
+    M, K = A.shape
+    N = B.shape[0]
+    C = torch.empty((M, N), dtype=torch.float32, device=A.device)
+    rc = L.odo_cnn_debug_gemm(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
+                              ctypes.c_void_p(C.data_ptr()), M, N, K, bn, layout,
+                              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise OdometryError(rc, "odo_cnn_debug_gemm: %s" % L.odo_status_string(rc).decode())
+    return C
+
+
+# ---------------------------------------------------------------- SE(3) helpers
+def motion_vec(T):
+    """(translation, rotation vector) 6-vector of a 4x4 rigid motion."""
+    from .synth import R_to_rotvec
+    T = np.asarray(T, np.float64)
+    return np.concatenate([T[:3, 3], R_to_rotvec(T[:3, :3])])
+
+
+def vec_motion(v):
+    from .synth import pose, rotvec_to_R
+    v = np.asarray(v, np.float64)
+    return pose(rotvec_to_R(v[3:]), v[:3])
+
+
+# ---------------------------------------------------------------- GPU-rendered frame pairs
+class PairSet:
+    """n frame pairs of one resolution resident on the GPU, stacked:
+    model prediction (vertices, normals, RGBA) at T1 and live frame (depth,
+    RGBA) at T2 = T1 * motion."""
+
+    def __init__(self, cam, T1, T2, model_vert, model_norm, model_rgba, depth, rgba):
+        self.cam, self.T1, self.T2 = cam, T1, T2
+        self.model_vert, self.model_norm, self.model_rgba = model_vert, model_norm, model_rgba
+        self.depth, self.rgba = depth, rgba
+        self.n = len(T1)
+
+    def frame_pairs(self, idx=None, levels=3, iterations=(0, 0, 0)):
+        from .batch import FramePair
+        idx = range(self.n) if idx is None else idx
+        return [FramePair(self.cam, self.model_vert[i], self.model_norm[i], self.model_rgba[i], self.depth[i],
+                          self.rgba[i], self.model_rgba[i], self.T1[i], levels=levels, iterations=iterations)
+                for i in idx]
+
+
+def render_views(scenes, view_scene, poses, seeds, cam, depth=True, rgba=True, model=False, noise_k=0.0012,
+                 dropout=0.05, min_mm=300, max_mm=5000):
+    """Renders len(poses) views on the GPU (odo_synth_render); returns a dict
+    of CUDA tensors 'depth' [n,h,w] uint16, 'rgba' [n,h,w,4] uint8 and, when
+    model, 'vert' / 'norm' [n,h,w,4] float32."""
+    import torch
+    from .synth import Scene
+    L = _native.load()
+    n, h, w = len(poses), cam.height, cam.width
+    sc = (Scene * len(scenes))(*scenes)
+    vs = np.ascontiguousarray(view_scene, np.int32)
+    ps = np.ascontiguousarray(np.asarray(poses, np.float32).reshape(n, 16))
+    sd = np.ascontiguousarray(seeds, np.uint64)
+    out = {}
+    dev = torch.device("cuda")
+    out["depth"] = torch.empty((n, h, w), dtype=torch.uint16, device=dev) if depth else None
+    out["rgba"] = torch.empty((n, h, w, 4), dtype=torch.uint8, device=dev) if rgba else None
+    out["vert"] = torch.empty((n, h, w, 4), dtype=torch.float32, device=dev) if model else None
+    out["norm"] = torch.empty((n, h, w, 4), dtype=torch.float32, device=dev) if model else None
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+    rc = L.odo_synth_render(ctypes.cast(sc, ctypes.c_void_p), len(scenes),
+                            vs.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                            ps.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                            sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n, w, h, cam.fx, cam.fy, cam.cx,
+                            cam.cy, noise_k, dropout, min_mm, max_mm, ptr(out["depth"]), ptr(out["rgba"]),
+                            ptr(out["vert"]), ptr(out["norm"]), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise OdometryError(rc, "odo_synth_render failed")
+    return {k: v for k, v in out.items() if v is not None}
+
+
+def make_room_pairs(seed, n, cam=None, max_deg=10.0, max_m=0.10, nscenes=64):
+    """n seeded room pairs (6x4x3 m rooms, 20 spheres) rendered on the GPU:
+    camera near the room centre, live frame at a random relative motion of at
+    most max_deg / max_m."""
+    from . import synth
+    cam = cam or synth.Camera()
+    rng = np.random.default_rng(seed)
+    scenes = [synth.make_room(seed * 7919 + k, 20) for k in range(nscenes)]
+    view_scene = rng.integers(0, nscenes, size=n)
+    T1 = np.stack([synth.room_camera(rng) for _ in range(n)])
+    T2 = np.stack([T1[i] @ synth.random_motion(rng, max_deg, max_m) for i in range(n)])
+    seeds = rng.integers(1, 2 ** 62, size=n, dtype=np.uint64)
+    m = render_views(scenes, view_scene, T1, seeds, cam, depth=False, rgba=True, model=True)
+    lv = render_views(scenes, view_scene, T2, seeds + np.uint64(1), cam, depth=True, rgba=True, model=False)
+    return PairSet(cam, T1, T2, m["vert"], m["norm"], m["rgba"], lv["depth"], lv["rgba"])
+
+
+# ---------------------------------------------------------------- labelling, inputs, training
+def track_plain(batch, pairset, idx, levels=3, iterations=(0, 0, 0)):
+    """Plain tracking (SO3 + ICP + RGB, the reference schedule) of pairs idx."""
+    return batch.track(pairset.frame_pairs(idx, levels=levels, iterations=iterations))
+
+
+def label_pairs(batch, pairset, chunk=512, agree_deg=1.0, agree_m=0.02):
+    """Labels = the plain tracker's relative motion T1^-1 T_icp per pair, and
+    a mask of the pairs where the plain tracker converged (its result within
+    agree_deg / agree_m of the rendering pose)."""
+    from .batch import result_pose
+    from .synth import pose_error
+    labels = np.zeros((pairset.n, 6), np.float32)
+    ok = np.zeros(pairset.n, bool)
+    for s in range(0, pairset.n, chunk):
+        idx = list(range(s, min(pairset.n, s + chunk)))
+        res = track_plain(batch, pairset, idx)
+        for i, r in zip(idx, res):
+            T = result_pose(r)
+            labels[i] = motion_vec(np.linalg.inv(pairset.T1[i]) @ T)
+            e = pose_error(T, pairset.T2[i])
+            ok[i] = e[0] <= np.radians(agree_deg) and e[1] <= agree_m
+    return labels, ok
+
+
+def pack_inputs(net, pairset, out=None, chunk=None):
+    """Network inputs [n,120,160,8] float16 of all pairs of a PairSet."""
+    import torch
+    if out is None:
+        out = torch.empty((pairset.n, IN_H, IN_W, IN_C), dtype=torch.float16, device="cuda")
+    chunk = chunk or net.max_batch
+    fps = pairset.frame_pairs()
+    for s in range(0, pairset.n, chunk):
+        net.pack(fps[s:s + chunk], out[s:s + chunk])
+    return out
+
+
+def train(net, inputs, labels, epochs=20, batch=256, lr=1e-3, lr_final=1e-4, seed=0, log=None):
+    """Adam on shuffled mini-batches (the network's own CUDA kernels);
+    cosine learning-rate decay from lr to lr_final.  Returns the mean loss of
+    every epoch."""
+    import torch
+    n = inputs.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    steps = epochs * (n // batch)
+    hist, k = [], 0
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g).cuda()
+        tot = 0.0
+        for s in range(0, n - batch + 1, batch):
+            sel = perm[s:s + batch]
+            x = inputs.index_select(0, sel).contiguous()
+            y = labels.index_select(0, sel).contiguous()
+            cur = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * k / max(1, steps)))
+            want = (s + 2 * batch > n)
+            l = net.train_step(x, y, cur, want_loss=want)
+            k += 1
+            if want:
+                tot = l
+        hist.append(tot)
+        if log:
+            log("epoch %d loss %.5f" % (ep, tot))
+    return hist
