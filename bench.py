@@ -51,12 +51,22 @@ def parse():
     ap.add_argument("--mode", default="graph", choices=["graph", "stream", "persistent"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--study", default=None, choices=[None, "batch", "precision"],
+    ap.add_argument("--study", default=None, choices=[None, "batch", "precision", "warm"],
                     help="batch: 512 mixed-resolution pairs per launch (batched verification); "
                          "precision: 1000 corridor pairs, FP32 vs compensated FP32 vs the FP64 oracle")
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
+    ap.add_argument("--train-pairs", type=int, default=50000, help="warm study: rendered training pairs")
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--eval-pairs", type=int, default=2000)
+    ap.add_argument("--warm-levels", type=int, default=3)
+    ap.add_argument("--warm-iters", default="6,4,4")
+    ap.add_argument("--max-disagree", type=float, default=5.0, help="warm study: fall-back angle (deg)")
+    ap.add_argument("--oracle-pairs", type=int, default=24, help="warm study: pairs also tracked by the FP64 oracle")
+    ap.add_argument("--save-params", default=None)
+    ap.add_argument("--load-params", default=None, help="warm study: skip training, use these parameters")
+    ap.add_argument("--sweep", action="store_true", help="warm study: also evaluate other warm schedules")
     a = ap.parse_args()
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
@@ -579,8 +589,186 @@ def run_precision_study(args):
     print(json.dumps(out), flush=True)
 
 
+def _res_array(res):
+    """Poses [n,4,4], lastICPError [n], iterations [n,4] of a result array."""
+    n = len(res)
+    P = np.array([np.array(r.pose, np.float64).reshape(4, 4) for r in res]).reshape(n, 4, 4)
+    e = np.array([r.lastICPError for r in res], np.float64)
+    it = np.array([list(r.iterations) for r in res], np.int64).reshape(n, 4)
+    return P, e, it
+
+
+def _errs(P, T):
+    from slam_gb300 import synth
+    return np.array([synth.pose_error(P[i], T[i]) for i in range(len(P))]).reshape(len(P), 2)
+
+
+def run_warm_study(args):
+    """Learned warm start (batched) against the plain tracker on held-out
+    640x480 room pairs (motion <= 10 deg / 10 cm): the network is trained
+    here, on the GPU, by the library's own kernels, on pairs rendered on the
+    GPU and labelled by the plain tracker."""
+    import torch
+    from slam_gb300 import synth, warmstart as ws, RGBDOdometry, DEFAULT_ANGLE_THRESH, DEFAULT_DIST_THRESH
+    from slam_gb300.batch import BatchOdometry
+    torch.cuda.set_device(0)
+    cam = synth.Camera()
+    b = BatchOdometry(512)
+    net = ws.WarmStartNet(max_batch=256)
+    if args.load_params:
+        d = np.load(args.load_params)
+        net.set_params(d["params"])
+        plain_res, n_train, gen_s, train_s, hist = float(d["plain_residual"]), int(d["n_train"]), 0.0, 0.0, [None]
+    else:
+        t0 = time.time()
+        ts = ws.make_training_set(net, b, args.seed * 17 + 3, args.train_pairs)
+        torch.cuda.synchronize()
+        gen_s = time.time() - t0
+        net.set_loss_metric(ts["metric"])
+        t0 = time.time()
+        hist = ws.train(net, ts["inputs"], ts["labels"], epochs=args.epochs, batch=256, lr=1e-3, lr_final=3e-5)
+        torch.cuda.synchronize()
+        train_s = time.time() - t0
+        plain_res = float(np.median(ts["residuals"]))
+        n_train = int(ts["labels"].shape[0])
+        del ts
+        if args.save_params:
+            np.savez(args.save_params, params=net.get_params(), plain_residual=plain_res, n_train=n_train)
+    its = tuple(int(v) for v in args.warm_iters.split(","))
+    wkw = dict(levels=args.warm_levels, iterations=its, residual_limit=1.5 * plain_res,
+               max_disagree_deg=args.max_disagree)
+    chunk, reps = 500, 3
+    t_plain = t_warm = 0.0
+    rows = {"plain": [], "warm": []}
+    T2, fbs, props_err = [], [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream()
+    oracle_sets, single_fps = [], None
+    for c, s in enumerate(range(0, args.eval_pairs, chunk)):
+        m = min(chunk, args.eval_pairs - s)
+        ps = ws.make_room_pairs(args.seed * 31 + 1000 + c, m, cam, 10.0, 0.10)
+        fps = ps.frame_pairs()
+        descs = b._descs(fps)
+        if c == 0:
+            tuned = b.autotune(fps)                          # launch shape of both paths
+            prop = net.propose(fps).cpu().numpy().astype(np.float64)
+            gt = np.stack([ws.motion_vec(np.linalg.inv(ps.T1[i]) @ ps.T2[i]) for i in range(m)])
+            prop_err = (np.linalg.norm(prop[:, :3] - gt[:, :3], axis=1), np.linalg.norm(prop[:, 3:] - gt[:, 3:], axis=1))
+            sweep = []
+            if args.sweep:
+                rp0 = b.track(fps, descs=descs)
+                Pp0 = _res_array(rp0)[0]
+                for lv, it_ in ((1, (4, 0, 0)), (1, (6, 0, 0)), (2, (3, 3, 0)), (2, (5, 3, 0)), (3, (4, 3, 3)),
+                                (3, (6, 4, 4))):
+                    for dis in (3.0, 5.0, 10.0):
+                        kw = dict(wkw, levels=lv, iterations=it_, max_disagree_deg=dis)
+                        b.track_warm(net, fps, descs=descs, **kw)
+                        torch.cuda.synchronize()
+                        tt = time.perf_counter()
+                        rw0, fb0 = b.track_warm(net, fps, descs=descs, **kw)
+                        torch.cuda.synchronize()
+                        tt = time.perf_counter() - tt
+                        Pw0, ew0, _ = _res_array(rw0)
+                        ee = _errs(Pw0, ps.T2)
+                        sweep.append({"levels": lv, "iterations": list(it_), "max_disagree_deg": dis,
+                                      "fps": m / tt, "fallback": float(fb0.mean()),
+                                      "rot_p50": float(np.median(ee[:, 0])), "trans_p50": float(np.median(ee[:, 1])),
+                                      "fail": float(np.mean((ee[:, 0] > np.radians(2)) | (ee[:, 1] > 0.05)))})
+        rp = b.track(fps, descs=descs)                      # warm-up (graph instantiation)
+        rw, fb = b.track_warm(net, fps, descs=descs, **wkw)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            rp = b.track(fps, descs=descs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_plain += e0.elapsed_time(e1) / reps
+        e0.record(stream)
+        for _ in range(reps):
+            rw, fb = b.track_warm(net, fps, descs=descs, **wkw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_warm += e0.elapsed_time(e1) / reps
+        rows["plain"].append(_res_array(rp))
+        rows["warm"].append(_res_array(rw))
+        fbs.append(fb)
+        T2.append(ps.T2)
+        if c == 0 and args.oracle_pairs > 0:
+            k = min(args.oracle_pairs, m)
+            oracle_sets = [(ps.cam, ps.T1[i], ps.model_vert[i].cpu().numpy(), ps.model_norm[i].cpu().numpy(),
+                            ps.model_rgba[i].cpu().numpy(), ps.depth[i].view(torch.int16).cpu().numpy().view(np.uint16),
+                            ps.rgba[i].cpu().numpy()) for i in range(k)]
+            # the drop-in single-pair path on the same pairs
+            h = RGBDOdometry(cam.width, cam.height, cam.cx, cam.cy, cam.fx, cam.fy)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for i in range(k):
+                h.initFirstRGB(ps.model_rgba[i])
+                h.initICPModel(ps.model_vert[i], ps.model_norm[i], 20.0, ps.T1[i])
+                h.initRGBModel(ps.model_rgba[i])
+                h.initICP(ps.depth[i], 20.0)
+                h.initRGB(ps.rgba[i])
+                h.getIncrementalTransformation(ps.T1[i][:3, 3].astype(np.float32), ps.T1[i][:3, :3].astype(np.float32))
+            torch.cuda.synchronize()
+            single_fps = k / (time.perf_counter() - t)
+        del ps, fps
+    Pp, ep, itp = (np.concatenate([r[j] for r in rows["plain"]]) for j in range(3))
+    Pw, ew, itw = (np.concatenate([r[j] for r in rows["warm"]]) for j in range(3))
+    T2 = np.concatenate(T2)
+    fb = np.concatenate(fbs)
+    n = len(Pp)
+    err_p, err_w = _errs(Pp, T2), _errs(Pw, T2)
+    d = _errs(Pw, Pp)
+    fail = lambda e: float(np.mean((e[:, 0] > np.radians(2.0)) | (e[:, 1] > 0.05)))
+    pct = lambda v: {"p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90))}
+    judge = (ew > 1.5 * ep) | (d[:, 0] > np.radians(0.5))
+    # FP64 oracle on the first pairs (plain tracking of the same frames)
+    from oracle import oracle
+    orc = []
+    for i, (c_, T1, mv, mn, mc, dep, rgba) in enumerate(oracle_sets):
+        o = oracle.Odometry(c_.width, c_.height, c_.cx, c_.cy, c_.fx, c_.fy, DEFAULT_DIST_THRESH,
+                            DEFAULT_ANGLE_THRESH, prec=64)
+        o.initFirstRGB(mc)
+        o.initICPModel(mv, mn, 20.0, T1.astype(np.float32))
+        o.initRGBModel(mc)
+        o.initICP(dep, 20.0)
+        o.initRGB(rgba)
+        t, R = o.getIncrementalTransformation(T1[:3, 3], T1[:3, :3])
+        To = synth.pose(np.asarray(R, np.float64), np.asarray(t, np.float64))
+        o.close()
+        orc.append((synth.pose_error(Pp[i], To), synth.pose_error(Pw[i], To), synth.pose_error(To, T2[i])))
+    within = lambda k: float(np.mean([(x[k][0] <= 1e-5 and x[k][1] <= 1e-5) for x in orc])) if orc else None
+    out = {"study": "warm", "metric": "warm-started batched vs plain tracking frames/s @640x480, equal pose error",
+           "unit": "frames/s", "data": "synthetic",
+           "config": {"workload": f"{n} held-out room pairs 640x480 (6x4x3 m rooms, 20 spheres), motion <= 10 deg / "
+                                  "10 cm, batches of 500",
+                      "train": {"pairs_rendered": args.train_pairs, "pairs_kept": n_train, "epochs": args.epochs,
+                                "generation_s": gen_s, "train_s": train_s, "last_epoch_loss": hist[-1]},
+                      "warm_schedule": {"levels": args.warm_levels, "iterations": list(its), "so3": False},
+                      "fallback": {"residual_limit": 1.5 * plain_res, "max_disagree_deg": args.max_disagree}},
+           "plain_batched_fps": n / (t_plain * 1e-3), "warm_batched_fps": n / (t_warm * 1e-3),
+           "plain_single_pair_fps": single_fps,
+           "speedup_vs_plain_batched": t_plain / t_warm, "speedup_vs_plain_single": n / (t_warm * 1e-3) / single_fps,
+           "pose_error_vs_gt": {"plain": {"rot_rad": pct(err_p[:, 0]), "trans_m": pct(err_p[:, 1]), "fail": fail(err_p)},
+                                "warm": {"rot_rad": pct(err_w[:, 0]), "trans_m": pct(err_w[:, 1]), "fail": fail(err_w)}},
+           "warm_vs_plain": {"within_1e-5": float(np.mean((d[:, 0] <= 1e-5) & (d[:, 1] <= 1e-5))),
+                             "within_1e-4": float(np.mean((d[:, 0] <= 1e-4) & (d[:, 1] <= 1e-4))),
+                             "judged_disagreement_rate": float(np.mean(judge))},
+           "runtime_fallback_rate": float(np.mean(fb)),
+           "iterations_mean": {"plain": itp.mean(axis=0).tolist(), "warm": itw.mean(axis=0).tolist()},
+           "proposal_error_vs_gt": {"trans_m": pct(prop_err[0]), "rot_rad": pct(prop_err[1])},
+           "launch": {"threads": tuned[0], "pixels_per_thread": tuned[1]},
+           "loss_history": [h for h in hist if h is not None][-5:], "sweep": sweep,
+           "fp64_oracle": {"pairs": len(orc), "plain_within_1e-5": within(0), "warm_within_1e-5": within(1),
+                           "oracle_vs_gt_rot_p50": float(np.median([x[2][0] for x in orc])) if orc else None}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.study == "warm":
+        run_warm_study(args)
+        return
     if args.study == "batch":
         run_batch_study(args)
         return

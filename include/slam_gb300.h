@@ -301,9 +301,11 @@ int odo_icp_step_noalloc(const float *vmap_curr, const float *nmap_curr, const f
  * Input [B][120][160][8] FP16 NHWC: model depth (m), model gray (0..1), live
  * depth (m), live gray, four zero channels.  Output [B][6]: translation (m)
  * and rotation vector (rad) of the live camera in the model camera's frame.
- * Six 3x3/stride-2 convolutions (8->32->64->128->128->128->128, ReLU), fc
+ * Six 3x3/stride-2 convolutions (8->32->64->128->128->128->128, ReLU; the
+ * first one with FP16 operands, the others BF16), fc
  * 768->768 (ReLU), fc 768->6; odo_cnn_param_count() FP32 parameters.
- * Loss: mean over the batch of sum_i (scale_i (out_i - label_i))^2, Adam. */
+ * Loss: mean over the batch of e^T M e, e = out - label, M a symmetric 6x6
+ * metric (default diag(100, 100, 100, 36, 36, 36)); Adam. */
 typedef struct odo_cnn odo_cnn_t;
 size_t odo_cnn_param_count(void);
 int odo_cnn_create(int max_batch, odo_cnn_t **out);
@@ -312,7 +314,7 @@ int odo_cnn_set_stream(odo_cnn_t *n, void *stream);
 int odo_cnn_init_params(odo_cnn_t *n, uint64_t seed);          /* He-normal weights, zero biases */
 int odo_cnn_set_params(odo_cnn_t *n, const float *host_params); /* also resets the optimiser */
 int odo_cnn_get_params(odo_cnn_t *n, float *host_params);
-int odo_cnn_set_loss_scale(odo_cnn_t *n, const float scale[6]);
+int odo_cnn_set_loss_metric(odo_cnn_t *n, const float metric[36]); /* row-major, symmetric */
 /* out_dev (may be NULL): [batch][6] FP32 on the device */
 int odo_cnn_forward(odo_cnn_t *n, const uint16_t *input_dev, int batch, float *out_dev);
 /* Network inputs [npairs][120][160][8] of frame pairs whose level-0 size is
@@ -320,6 +322,14 @@ int odo_cnn_forward(odo_cnn_t *n, const uint16_t *input_dev, int batch, float *o
  * intensity and of the live depth and intensity (asynchronous, on the
  * network's stream). */
 int odo_cnn_pack_input(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t *input_dev);
+/* Motion proposals [npairs][6] (device) of frame pairs whose level-0 size is
+ * (160 s) x (120 s): packing and forward pass in chunks of the network's
+ * batch size, asynchronous on the network's stream; odo_cnn_event() is
+ * recorded at its end (a cudaEvent_t) and odo_cnn_wait() waits for it and
+ * reports a tensor-core time-out (ODO_ERR_TIMEOUT). */
+int odo_cnn_propose(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_dev);
+void *odo_cnn_event(odo_cnn_t *n);
+int odo_cnn_wait(odo_cnn_t *n);
 /* forward + loss + backward + Adam (beta 0.9/0.999, eps 1e-8); loss_host may be NULL (no sync) */
 int odo_cnn_train_step(odo_cnn_t *n, const uint16_t *input_dev, const float *labels_dev, int batch, float lr,
                        float *loss_host);
@@ -327,6 +337,24 @@ int odo_cnn_train_step(odo_cnn_t *n, const uint16_t *input_dev, const float *lab
 int odo_cnn_gradients(odo_cnn_t *n, const uint16_t *input_dev, const float *labels_dev, int batch,
                       float *grad_host, float *loss_host);
 const char *odo_cnn_last_error(odo_cnn_t *n);
+/* Learned warm start of batched tracking: proposals of the network for every
+ * pair, tracking from pose * exp(proposal) with the short schedule of `wp`
+ * (no SO3 stage), and a fall-back to the pair's own plain schedule (SO3 on)
+ * for the pairs whose final ICP residual exceeds wp->residual_limit or whose
+ * refined rotation differs from the proposal by more than wp->max_disagree
+ * (rad).  fallback (host, may be NULL) gets 1 for those pairs. */
+typedef struct {
+    int levels;            /* pyramid levels iterated after the warm start, 1..3 */
+    int iterations[3];     /* per-level iterations (0: the reference's 10 / 5 / 4) */
+    float residual_limit;  /* <= 0: no residual test */
+    float max_disagree;    /* rad; <= 0: no disagreement test */
+    int rgbOnly;
+    float icpWeight;
+    int fastOdom;
+} odo_warm_params;
+int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, int npairs,
+                         const odo_warm_params *wp, odo_pair_result *results, int *fallback);
+
 /* GPU ray caster of the synthetic test scenes (scene struct of the synthetic
  * data generator, synth_scene): view i of scene view_scene[i] at
  * camera-to-world pose poses[16 i .. 16 i + 15] (row-major), depth noise
@@ -339,8 +367,8 @@ int odo_synth_render(const void *scenes_host, int nscenes, const int *view_scene
                      float *vert_dev, float *norm_dev, void *stream);
 /* C[M][N] (FP32) = A[M][K] B[N][K]^T with BF16 A, B (rows padded to a
  * multiple of 8 elements) on the tensor-core GEMM; bn = tile width 32..256,
- * layout = 0 (the library's operand layout) or 1 (offsets exchanged; a
- * self-check of the layout). */
+ * layout = 0 (the library's operand layout), 1 (offsets exchanged; a
+ * self-check of the layout) or 2 (layout 0 with FP16 operands). */
 int odo_cnn_debug_gemm(const uint16_t *A_dev, const uint16_t *B_dev, float *C_dev, int M, int N, int K, int bn,
                        int layout, void *stream);
 

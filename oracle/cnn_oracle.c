@@ -7,10 +7,12 @@
  * with FP64 accumulation:
  *   input [B][120][160][8] FP16 NHWC, six 3x3 / stride 2 / pad 1 convolutions
  *   8->32->64->128->128->128->128 with ReLU, fc 768->768 ReLU, fc 768->6,
- *   loss = mean_b sum_i (s_i (out_i - label_i))^2.
- * rounding = 1 reproduces the GPU's rounding points (BF16 weights,
- * activations and activation gradients, FP32 sums, FP32 output / loss
- * gradient); rounding = 0 keeps everything in FP64 (for the finite-difference
+ *   loss = mean_b e^T M e, e = out - label, M a symmetric 6x6 metric.
+ * rounding = 1 reproduces the GPU's rounding points (FP16 input and FP16
+ * first-layer weights in the forward pass, BF16 weights, activations and
+ * activation gradients elsewhere -- the first layer's weight gradient uses
+ * the input rounded to BF16 --, FP32 sums, FP32 output / loss gradient);
+ * rounding = 0 keeps everything in FP64 (for the finite-difference
  * check of the backward formulas).  Only the order of the FP32 accumulations
  * inside the tensor cores is not reproduced (sums are exact in FP64 here). */
 #include <math.h>
@@ -60,6 +62,18 @@ static double rb(double x) {
     memcpy(&f, &u, 4);
     return (double)f;
 }
+/* FP32 value -> nearest FP16 (ties to even, subnormals kept), as double */
+static double rh(double x) {
+    if (!g_round) return x;
+    float f = (float)x;
+    const double a = fabs((double)f);
+    if (!(a < 65520.0)) return f > 0 ? INFINITY : -INFINITY;
+    int e;
+    frexp(a, &e);
+    const double q = a >= ldexp(1.0, -14) ? ldexp(1.0, e - 11) : ldexp(1.0, -24);
+    const double r = nearbyint(a / q) * q;
+    return f < 0 ? -r : r;
+}
 static double half_to_double(uint16_t h) {
     const int s = (h >> 15) & 1, e = (h >> 10) & 31, m = h & 1023;
     double v;
@@ -82,7 +96,7 @@ static long conv_src(int l, int B, int m, int k) {
 
 /* Forward, loss and (grad != NULL) backward.  params: FP32 parameter values
  * (as doubles); labels [B][6]; out [B][6]; grad in the parameter layout. */
-int cnn_oracle_run(const double *params, const uint16_t *input, const double *labels, const double *scale, int B,
+int cnn_oracle_run(const double *params, const uint16_t *input, const double *labels, const double *metric, int B,
                    int rounding, double *out, double *loss, double *grad) {
     g_round = rounding;
     size_t wo[NLAYERS], bo[NLAYERS], total;
@@ -90,14 +104,20 @@ int cnn_oracle_run(const double *params, const uint16_t *input, const double *la
     double *w = malloc(total * sizeof(double));
     for (size_t i = 0; i < total; ++i) w[i] = rb(params[i]); /* BF16 weights (biases use params directly) */
     double *act[NCONV + 1];
-    act[0] = malloc((size_t)B * IN_H * IN_W * IN_C * sizeof(double));
-    for (size_t i = 0; i < (size_t)B * IN_H * IN_W * IN_C; ++i) act[0][i] = rb(half_to_double(input[i]));
+    const size_t nin = (size_t)B * IN_H * IN_W * IN_C;
+    act[0] = malloc(nin * sizeof(double));      /* BF16 view of the input (first-layer weight gradient) */
+    double *in16 = malloc(nin * sizeof(double)); /* the FP16 input (first-layer forward product) */
+    for (size_t i = 0; i < nin; ++i) {
+        in16[i] = half_to_double(input[i]);
+        act[0][i] = rb(in16[i]);
+    }
+    for (size_t i = 0; i < (size_t)COUT[0] * 9 * CIN[0]; ++i) w[wo[0] + i] = rh(params[wo[0] + i]);
     /* convolutions */
     for (int l = 0; l < NCONV; ++l) {
         const int M = B * HH[l + 1] * WW[l + 1], N = COUT[l], K = 9 * CIN[l];
         act[l + 1] = malloc((size_t)M * N * sizeof(double));
         double *y = act[l + 1];
-        const double *x = act[l];
+        const double *x = l == 0 ? in16 : act[l];
 #pragma omp parallel for schedule(static)
         for (int m = 0; m < M; ++m)
             for (int n = 0; n < N; ++n) {
@@ -130,11 +150,15 @@ int cnn_oracle_run(const double *params, const uint16_t *input, const double *la
     /* loss and its gradient */
     double *dout = malloc((size_t)B * NOUT * sizeof(double));
     double L = 0;
-    for (int i = 0; i < B * NOUT; ++i) {
-        const double s = rf(scale[i % NOUT]);
-        const double d = rf(out[i] - labels[i]);
-        L += s * s * d * d;
-        dout[i] = rf(rf(rf(rf(2.0 * s) * s) * d) / (double)B);
+    for (int bb = 0; bb < B; ++bb) {
+        double e[NOUT];
+        for (int i = 0; i < NOUT; ++i) e[i] = rf(out[bb * NOUT + i] - labels[bb * NOUT + i]);
+        for (int i = 0; i < NOUT; ++i) {
+            double me = 0;
+            for (int j = 0; j < NOUT; ++j) me = rf(me + rf(metric[i * NOUT + j]) * e[j]);
+            L += e[i] * me;
+            dout[bb * NOUT + i] = rf(rf(2.0 * me) / (double)B);
+        }
     }
     *loss = L / B;
     if (!grad) goto done;
@@ -236,6 +260,7 @@ int cnn_oracle_run(const double *params, const uint16_t *input, const double *la
     }
 done:
     for (int l = 0; l <= NCONV; ++l) free(act[l]);
+    free(in16);
     free(hid);
     free(dout);
     free(w);

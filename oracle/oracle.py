@@ -345,15 +345,16 @@ def cnn_layout():
     return list(w), list(b), t.value
 
 
-def cnn_run(params, inputs_f16, labels, scale, rounding=True, want_grad=True):
+def cnn_run(params, inputs_f16, labels, metric, rounding=True, want_grad=True):
     """Forward + loss (+ gradients) of the warm-start network on the CPU.
     params: FP32 parameter vector; inputs_f16: uint16 [B,120,160,8] (FP16
-    bits); labels [B,6].  Returns (out [B,6], loss, grad or None)."""
+    bits); labels [B,6]; metric: 6x6 loss metric.  Returns (out [B,6], loss,
+    grad or None)."""
     p = np.ascontiguousarray(params, np.float64)
     x = np.ascontiguousarray(inputs_f16, np.uint16)
     B = x.shape[0]
     lab = np.ascontiguousarray(labels, np.float64).reshape(B, 6)
-    sc = np.ascontiguousarray(scale, np.float64).reshape(6)
+    sc = np.ascontiguousarray(metric, np.float64).reshape(36)
     out = np.zeros((B, 6), np.float64)
     loss = ctypes.c_double()
     grad = np.zeros_like(p) if want_grad else None

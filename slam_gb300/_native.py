@@ -75,6 +75,11 @@ class OdoPairResult(ctypes.Structure):
                 ("lastA", c_double * 36), ("lastb", c_double * 6)]
 
 
+class OdoWarmParams(ctypes.Structure):
+    _fields_ = [("levels", c_int), ("iterations", c_int * 3), ("residual_limit", c_float),
+                ("max_disagree", c_float), ("rgbOnly", c_int), ("icpWeight", c_float), ("fastOdom", c_int)]
+
+
 # (name, restype, argtypes) of every function declared in include/slam_gb300.h
 SIGNATURES = [
     ("odo_create", c_int, [c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_float, P(c_void_p)]),
@@ -116,13 +121,18 @@ SIGNATURES = [
     ("odo_cnn_init_params", c_int, [c_void_p, ctypes.c_uint64]),
     ("odo_cnn_set_params", c_int, [c_void_p, P(c_float)]),
     ("odo_cnn_get_params", c_int, [c_void_p, P(c_float)]),
-    ("odo_cnn_set_loss_scale", c_int, [c_void_p, P(c_float)]),
+    ("odo_cnn_set_loss_metric", c_int, [c_void_p, P(c_float)]),
     ("odo_cnn_forward", c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     ("odo_cnn_train_step", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_float, P(c_float)]),
     ("odo_cnn_pack_input", c_int, [c_void_p, P(OdoPair), c_int, c_void_p]),
     ("odo_synth_render", c_int, [c_void_p, c_int, P(c_int), P(c_float), P(ctypes.c_uint64), c_int, c_int, c_int,
                                  c_float, c_float, c_float, c_float, c_float, c_float, c_int, c_int, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("odo_cnn_propose", c_int, [c_void_p, P(OdoPair), c_int, c_void_p]),
+    ("odo_cnn_event", c_void_p, [c_void_p]),
+    ("odo_cnn_wait", c_int, [c_void_p]),
+    ("odo_batch_track_warm", c_int, [c_void_p, c_void_p, P(OdoPair), c_int, P(OdoWarmParams), P(OdoPairResult),
+                                     P(c_int)]),
     ("odo_cnn_gradients", c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_float), P(c_float)]),
     ("odo_cnn_last_error", ctypes.c_char_p, [c_void_p]),
     ("odo_cnn_debug_gemm", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),

@@ -109,6 +109,27 @@ class BatchOdometry:
                     "odo_batch_track_init")
         return res
 
+    def track_warm(self, net, pairs, levels=2, iterations=(4, 3, 0), residual_limit=0.0, max_disagree_deg=0.0,
+                   rgbOnly=False, icpWeight=10.0, fastOdom=False, descs=None):
+        """Learned warm start (odo_batch_track_warm): the network's proposal
+        per pair, tracking with the short schedule, fall-back to the plain
+        schedule where the residual or the disagreement test fails.  Returns
+        (results, fallback mask)."""
+        descs = descs if descs is not None else self._descs(pairs)
+        n = len(descs)
+        res = (_native.OdoPairResult * n)()
+        fb = (ctypes.c_int * n)()
+        wp = _native.OdoWarmParams()
+        wp.levels = int(levels)
+        for l in range(3):
+            wp.iterations[l] = int(iterations[l])
+        wp.residual_limit = float(residual_limit)
+        wp.max_disagree = float(np.radians(max_disagree_deg))
+        wp.rgbOnly, wp.icpWeight, wp.fastOdom = int(bool(rgbOnly)), float(icpWeight), int(bool(fastOdom))
+        self._check(self._L.odo_batch_track_warm(self._h, net._h, descs, n, ctypes.byref(wp), res, fb),
+                    "odo_batch_track_warm")
+        return res, np.array(fb[:], bool)
+
     def autotune(self, pairs, rgbOnly=False, icpWeight=10.0, fastOdom=False, so3=True):
         descs = self._descs(pairs)
         res = (_native.OdoPairResult * len(pairs))()

@@ -59,6 +59,7 @@ struct odo_batch {
     size_t arena_bytes = 0;
     Layout layout;
     std::vector<PairBufs> bufs;
+    std::vector<int> slot;  // pair i of the current call uses bufs[slot[i]]
     unsigned char *args_dev = nullptr, *args_host = nullptr;  // host pinned
     size_t args_bytes = 0;
     TrackState *st_dev = nullptr, *st_host = nullptr;           // host pinned
@@ -125,7 +126,31 @@ int blocks_for(const odo_batch_t *b, int n) {
 int ensure_layout(odo_batch_t *b, const odo_pair *pairs, int n) {
     Layout lay;
     for (int i = 0; i < n; ++i) lay.emplace_back(pairs[i].width, pairs[i].height);
-    if (lay == b->layout && b->arena) return ODO_OK;
+    b->slot.resize(n);
+    if (lay == b->layout && b->arena) {
+        for (int i = 0; i < n; ++i) b->slot[i] = i;
+        return ODO_OK;
+    }
+    // a call with fewer pairs reuses free slots of the same size (no new arena)
+    if (b->arena && n < (int)b->layout.size()) {
+        std::vector<char> used(b->layout.size(), 0);
+        bool ok = true;
+        for (int i = 0; i < n && ok; ++i) {
+            int s = -1;
+            for (size_t j = 0; j < b->layout.size(); ++j)
+                if (!used[j] && b->layout[j] == lay[i]) {
+                    s = (int)j;
+                    break;
+                }
+            if (s < 0) ok = false;
+            else {
+                used[s] = 1;
+                b->slot[i] = s;
+            }
+        }
+        if (ok) return ODO_OK;
+    }
+    for (int i = 0; i < n; ++i) b->slot[i] = i;
     BCK(cudaStreamSynchronize(b->stream));
     drop_graphs(b);
     if (b->arena) cudaFree(b->arena);
@@ -211,7 +236,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
     for (int i = 0; i < kLevels; ++i) b->max_nb[i] = 1;
     for (int i = 0; i < n; ++i) {
         const odo_pair &q = pairs[i];
-        PairBufs &p = b->bufs[i];
+        PairBufs &p = b->bufs[b->slot[i]];
         const Intr K0{q.fx, q.fy, q.cx, q.cy};
         auto intr = [&](int l) {
             int div = 1 << l;
@@ -467,8 +492,11 @@ int odo_batch_set_launch(odo_batch_t *b, int threads, int pixels_per_thread) {
 
 namespace {
 
+// graph = false enqueues the kernels directly (for one-off batch sizes, e.g.
+// the fall-back subset of a warm-started batch, where instantiating a graph
+// would cost more than it saves).
 int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init, int rgbOnly, float icpWeight,
-               int fastOdom, int so3, odo_pair_result *results) {
+               int fastOdom, int so3, odo_pair_result *results, bool graph = true) {
     if (!b || !pairs || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
     for (int i = 0; i < npairs; ++i) {
         const odo_pair &q = pairs[i];
@@ -494,26 +522,31 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
             const int it = pairs[i].iterations[l] > 0 ? pairs[i].iterations[l] : base[l];
             if (it > max_iters[l]) max_iters[l] = it;
         }
-    if (warm) BCK(cudaMemcpyAsync(b->init_dev, init, sizeof(float) * 6 * npairs, cudaMemcpyDeviceToDevice, b->stream));
-    GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt};
-    auto it = b->graphs.find(key);
-    if (it == b->graphs.end()) {
-        cudaGraph_t g = nullptr;
-        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters);
-        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
-        if (e != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return bfail(b, e, "enqueue_batch (capture)");
+    if (warm && init != b->init_dev)
+        BCK(cudaMemcpyAsync(b->init_dev, init, sizeof(float) * 6 * npairs, cudaMemcpyDeviceToDevice, b->stream));
+    if (!graph) {
+        BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters));
+    } else {
+        GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt};
+        auto it = b->graphs.find(key);
+        if (it == b->graphs.end()) {
+            cudaGraph_t g = nullptr;
+            BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters);
+            cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+            if (e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return bfail(b, e, "enqueue_batch (capture)");
+            }
+            if (e2 != cudaSuccess) return bfail(b, e2, "cudaStreamEndCapture");
+            cudaGraphExec_t ex = nullptr;
+            e = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return bfail(b, e, "cudaGraphInstantiate");
+            it = b->graphs.emplace(key, ex).first;
         }
-        if (e2 != cudaSuccess) return bfail(b, e2, "cudaStreamEndCapture");
-        cudaGraphExec_t ex = nullptr;
-        e = cudaGraphInstantiate(&ex, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return bfail(b, e, "cudaGraphInstantiate");
-        it = b->graphs.emplace(key, ex).first;
+        BCK(cudaGraphLaunch(it->second, b->stream));
     }
-    BCK(cudaGraphLaunch(it->second, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     for (int i = 0; i < npairs; ++i) {
         const TrackState &st = b->st_host[i];
@@ -553,6 +586,59 @@ int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, cons
                          float icpWeight, int fastOdom, odo_pair_result *results) {
     if (!init_dev) return ODO_ERR_ARG;
     return track_impl(b, pairs, npairs, init_dev, rgbOnly, icpWeight, fastOdom, 0, results);
+}
+
+int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, int npairs,
+                         const odo_warm_params *wp, odo_pair_result *results, int *fallback) {
+    if (!b || !net || !pairs || !wp || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
+    if (wp->levels < 1 || wp->levels > 3) return ODO_ERR_ARG;
+    // 1. proposals straight into the warm-start buffer (network stream), then
+    //    the batch stream waits for them
+    int rc = odo_cnn_propose(net, pairs, npairs, b->init_dev);
+    if (rc != ODO_OK) return rc;
+    BCK(cudaStreamWaitEvent(b->stream, (cudaEvent_t)odo_cnn_event(net), 0));
+    // 2. tracking from the proposals with the short schedule
+    std::vector<odo_pair> warm(pairs, pairs + npairs);
+    for (auto &q : warm) {
+        q.levels = wp->levels;
+        for (int l = 0; l < kLevels; ++l) q.iterations[l] = wp->iterations[l];
+    }
+    rc = track_impl(b, warm.data(), npairs, b->init_dev, wp->rgbOnly, wp->icpWeight, wp->fastOdom, 0, results);
+    const int rc2 = odo_cnn_wait(net);
+    if (rc != ODO_OK) return rc;
+    if (rc2 != ODO_OK) return rc2;
+    // 3. fall-back decisions on the host: residual, and the angle between the
+    //    refined rotation and the proposed one, R_prop = R_pose exp(w)
+    std::vector<float> prop((size_t)6 * npairs);
+    BCK(cudaMemcpy(prop.data(), b->init_dev, prop.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    std::vector<int> idx;
+    for (int i = 0; i < npairs; ++i) {
+        bool fb = wp->residual_limit > 0 && !(results[i].lastICPError <= wp->residual_limit);
+        if (!fb && wp->max_disagree > 0) {
+            double w[3] = {prop[6 * i + 3], prop[6 * i + 4], prop[6 * i + 5]}, Rr[9], Rp[9], Rq[9];
+            se3::rodrigues(w, Rr);
+            for (int k = 0; k < 9; ++k) Rp[k] = pairs[i].pose[(k / 3) * 4 + k % 3];
+            se3::mm33(Rp, Rr, Rq);
+            // cos(angle) = (trace(R_res^T R_prop) - 1) / 2
+            double tr = 0;
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) tr += (double)results[i].pose[r * 4 + c] * Rq[r * 3 + c];
+            const double cs = 0.5 * (tr - 1.0);
+            fb = cs < std::cos((double)wp->max_disagree);
+        }
+        if (fallback) fallback[i] = fb ? 1 : 0;
+        if (fb) idx.push_back(i);
+    }
+    if (idx.empty()) return ODO_OK;
+    // 4. the pairs that fell back: plain schedule with the SO3 stage
+    std::vector<odo_pair> sub;
+    for (int i : idx) sub.push_back(pairs[i]);
+    std::vector<odo_pair_result> sres(idx.size());
+    rc = track_impl(b, sub.data(), (int)sub.size(), nullptr, wp->rgbOnly, wp->icpWeight, wp->fastOdom, 1, sres.data(),
+                    false);
+    if (rc != ODO_OK) return rc;
+    for (size_t k = 0; k < idx.size(); ++k) results[idx[k]] = sres[k];
+    return ODO_OK;
 }
 
 int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,

@@ -112,8 +112,10 @@ struct ConvGeo {
         return (((long long)b * H + iy) * W + ix) * C + ci;
     }
 };
-// Implicit im2col A(m, k) of a BF16 (or FP16 when F16) NHWC input; C % 8 == 0
-// so the 8 values of a K group share one tap.
+// Implicit im2col A(m, k) of an NHWC input; C % 8 == 0 so the 8 values of a
+// K group share one tap.  F16: the input is FP16 and is converted to BF16.
+// (With F16 false the 16-bit values pass through unchanged: BF16 for the BF16
+// GEMM, or FP16 for the FP16 GEMM of the first layer.)
 template <bool F16>
 struct LdIm2col {
     const uint16_t *x;
@@ -155,6 +157,11 @@ struct LdIm2colT {
 };
 
 // -------------------------------------------------------------- epilogues
+__device__ __forceinline__ uint16_t f2h(float f) {
+    __half h = __float2half_rn(f);
+    return *reinterpret_cast<uint16_t *>(&h);
+}
+
 struct EpBiasAct {  // y = act(v + bias) as BF16
     uint16_t *y;
     const float *bias;
@@ -265,15 +272,20 @@ __global__ void k_colsum(const T *g, int M, int N, int ld, float *db) {
     }
 }
 
-// loss = mean_b sum_i (s_i (out - label))^2 ; dout = d loss / d out
-__global__ void k_loss(const float *out, const float *label, const float *scale, int B, float *dout, float *loss) {
+// loss = mean_b e_b^T M e_b with e = out - label and a symmetric 6x6 metric
+// M; dout = d loss / d out = 2 M e / B
+__global__ void k_loss(const float *out, const float *label, const float *metric, int B, float *dout, float *loss) {
     __shared__ float red[256];
     float acc = 0.f;
-    for (int i = threadIdx.x; i < B * kOut; i += blockDim.x) {
-        const float s = scale[i % kOut];
-        const float d = out[i] - label[i];
-        acc += s * s * d * d;
-        dout[i] = 2.f * s * s * d / (float)B;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        float e[kOut];
+        for (int i = 0; i < kOut; ++i) e[i] = out[b * kOut + i] - label[b * kOut + i];
+        for (int i = 0; i < kOut; ++i) {
+            float me = 0.f;
+            for (int j = 0; j < kOut; ++j) me += metric[i * kOut + j] * e[j];
+            acc += e[i] * me;
+            dout[b * kOut + i] = 2.f * me / (float)B;
+        }
     }
     red[threadIdx.x] = acc;
     __syncthreads();
@@ -299,6 +311,10 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, size_t n, f
 __global__ void k_to_bf16(const float *p, uint16_t *q, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         q[i] = f2bf(p[i]);
+}
+__global__ void k_to_f16(const float *p, uint16_t *q, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        q[i] = f2h(p[i]);
 }
 // wt[c][r] = w[r][c] (BF16), rows padded with zeros up to ldt
 __global__ void k_transpose_bf16(const uint16_t *w, int rows, int cols, uint16_t *wt, int ldt) {
@@ -364,11 +380,11 @@ int grid_for(long long n, int threads) {
 // Conv layer l geometry for batch B.
 ConvGeo conv_geo(int l, int B) { return ConvGeo{B, kH[l], kW[l], kCin[l], kH[l + 1], kW[l + 1]}; }
 
-template <class LA, class LB, class EP>
+template <bool F16 = false, class LA, class LB, class EP>
 cudaError_t gemm(const LA &a, const LB &b, const EP &e, int M, int N, int K, int splits, int *err, cudaStream_t s) {
-    if (N <= 32) return launch_umma_gemm<32>(a, b, e, M, N, K, splits, 0, err, s);
-    if (N <= 64) return launch_umma_gemm<64>(a, b, e, M, N, K, splits, 0, err, s);
-    return launch_umma_gemm<128>(a, b, e, M, N, K, splits, 0, err, s);
+    if (N <= 32) return launch_umma_gemm<32, LA, LB, EP, F16>(a, b, e, M, N, K, splits, 0, err, s);
+    if (N <= 64) return launch_umma_gemm<64, LA, LB, EP, F16>(a, b, e, M, N, K, splits, 0, err, s);
+    return launch_umma_gemm<128, LA, LB, EP, F16>(a, b, e, M, N, K, splits, 0, err, s);
 }
 
 }  // namespace
@@ -384,10 +400,10 @@ cudaError_t cnn_forward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
     for (int l = 0; l < kConv; ++l) {
         const ConvGeo g = conv_geo(l, B);
         const int M = B * g.Ho * g.Wo, N = kCout[l], K = 9 * kCin[l];
-        const LdDense wb{n.wbf + P.w[l], N, K, K};
         const EpBiasAct ep{n.act[l + 1], n.master + P.b[l], N, N, 1};
-        if (l == 0) CNN_CK(gemm(LdIm2col<true>{input, g}, wb, ep, M, N, K, 1, n.err, s));
-        else CNN_CK(gemm(LdIm2col<false>{n.act[l], g}, wb, ep, M, N, K, 1, n.err, s));
+        // the first layer in FP16 (the FP16 depth keeps 11 significant bits)
+        if (l == 0) CNN_CK(gemm<true>(LdIm2col<false>{input, g}, LdDense{n.wh, N, K, K}, ep, M, N, K, 1, n.err, s));
+        else CNN_CK(gemm(LdIm2col<false>{n.act[l], g}, LdDense{n.wbf + P.w[l], N, K, K}, ep, M, N, K, 1, n.err, s));
     }
     const int l1 = kConv, l2 = kConv + 1;
     CNN_CK(gemm(LdDense{n.act[kConv], B, kFlat, kFlat}, LdDense{n.wbf + P.w[l1], kHidden, kFlat, kFlat},
@@ -404,7 +420,7 @@ cudaError_t cnn_pack(const PackArgs *args_dev, int n, uint16_t *out, cudaStream_
 }
 
 cudaError_t cnn_loss(Net &n, const float *labels, int B, cudaStream_t s) {
-    k_loss<<<1, 256, 0, s>>>(n.out, labels, n.scale, B, n.dout, n.loss);
+    k_loss<<<1, 256, 0, s>>>(n.out, labels, n.metric, B, n.dout, n.loss);
     return cudaGetLastError();
 }
 
@@ -465,6 +481,9 @@ cudaError_t cnn_adam(Net &n, float lr, float beta1, float beta2, float eps, cuda
 cudaError_t cnn_refresh_weights(Net &n, cudaStream_t s) {
     k_to_bf16<<<grid_for((long long)n.L.total, 256), 256, 0, s>>>(n.master, n.wbf, n.L.total);
     CNN_CK(cudaGetLastError());
+    const size_t n0 = (size_t)w_rows(0) * w_cols(0);
+    k_to_f16<<<grid_for((long long)n0, 256), 256, 0, s>>>(n.master + n.L.w[0], n.wh, n0);
+    CNN_CK(cudaGetLastError());
     for (int l = 0; l < kLayers; ++l) {
         const long long ne = (long long)w_cols(l) * n.L.wt_ld[l];
         k_transpose_bf16<<<grid_for(ne, 256), 256, 0, s>>>(n.wbf + n.L.w[l], w_rows(l), w_cols(l), n.wt + n.L.wt[l],
@@ -478,6 +497,12 @@ cudaError_t cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M
                            int *err, cudaStream_t s) {
     const LdDense la{A, M, K, (K + 7) & ~7}, lb{B, N, K, (K + 7) & ~7};
     const EpStore ep{C, N, N};
+    if (layout == 2) {  // FP16 operands
+        if (bn == 32) return launch_umma_gemm<32, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
+        if (bn == 64) return launch_umma_gemm<64, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
+        if (bn == 128) return launch_umma_gemm<128, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
+        return launch_umma_gemm<256, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
+    }
     if (bn == 32) return launch_umma_gemm<32>(la, lb, ep, M, N, K, 1, layout, err, s);
     if (bn == 64) return launch_umma_gemm<64>(la, lb, ep, M, N, K, 1, layout, err, s);
     if (bn == 128) return launch_umma_gemm<128>(la, lb, ep, M, N, K, 1, layout, err, s);

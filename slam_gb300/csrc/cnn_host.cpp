@@ -25,6 +25,9 @@ struct odo_cnn {
     PackArgs *pack_host = nullptr;  // pinned staging of the packer's per-pair arguments
     PackArgs *pack_dev = nullptr;
     cudaEvent_t pack_done = nullptr;  // the staging buffer is free again once this has fired
+    uint16_t *in_buf = nullptr;       // network inputs of odo_cnn_propose (max_batch pairs)
+    int *flag_host = nullptr;         // pinned copy of the time-out flag of the last proposal
+    cudaEvent_t done = nullptr;       // end of the last proposal
 };
 
 namespace {
@@ -121,6 +124,7 @@ int odo_cnn_create(int max_batch, odo_cnn_t **out) {
         return r;
     };
     const size_t P = N.L.total;
+    const size_t o_wh = take((size_t)w_rows(0) * w_cols(0) * 2);
     const size_t o_master = take(P * 4), o_wbf = take(P * 2), o_wt = take(N.L.wt_total * 2), o_grad = take(P * 4),
                  o_m = take(P * 4), o_v = take(P * 4);
     size_t o_act[kConv + 1] = {}, o_dpre[kConv + 1] = {};
@@ -135,7 +139,7 @@ int odo_cnn_create(int max_batch, odo_cnn_t **out) {
         if (d > dcol) dcol = d;
     }
     const size_t o_hid = take(B * kHidden * 2), o_dhid = take(B * kHidden * 2), o_out = take(B * kOut * 4),
-                 o_dout = take(B * kOut * 4), o_dcol = take(dcol * 4), o_loss = take(4), o_scale = take(kOut * 4),
+                 o_dout = take(B * kOut * 4), o_dcol = take(dcol * 4), o_loss = take(4), o_metric = take(kOut * kOut * 4),
                  o_err = take(4);
     if ((e = cudaMalloc(&n->arena, o)) != cudaSuccess) return bail(e, "cudaMalloc(cnn arena)");
     if ((e = cudaMemset(n->arena, 0, o)) != cudaSuccess) return bail(e, "cudaMemset(cnn arena)");
@@ -143,6 +147,7 @@ int odo_cnn_create(int max_batch, odo_cnn_t **out) {
     N.master = (float *)(a + o_master);
     N.wbf = (uint16_t *)(a + o_wbf);
     N.wt = (uint16_t *)(a + o_wt);
+    N.wh = (uint16_t *)(a + o_wh);
     N.grad = (float *)(a + o_grad);
     N.adam_m = (float *)(a + o_m);
     N.adam_v = (float *)(a + o_v);
@@ -156,15 +161,21 @@ int odo_cnn_create(int max_batch, odo_cnn_t **out) {
     N.dout = (float *)(a + o_dout);
     N.dcol = (float *)(a + o_dcol);
     N.loss = (float *)(a + o_loss);
-    N.scale = (float *)(a + o_scale);
+    N.metric = (float *)(a + o_metric);
     N.err = (int *)(a + o_err);
     if ((e = cudaMallocHost(&n->pack_host, sizeof(PackArgs) * B)) != cudaSuccess) return bail(e, "cudaMallocHost");
     if ((e = cudaMalloc(&n->pack_dev, sizeof(PackArgs) * B)) != cudaSuccess) return bail(e, "cudaMalloc(pack)");
     if ((e = cudaEventCreateWithFlags(&n->pack_done, cudaEventDisableTiming)) != cudaSuccess)
         return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&n->done, cudaEventDisableTiming)) != cudaSuccess)
+        return bail(e, "cudaEventCreate");
+    if ((e = cudaMallocHost(&n->flag_host, sizeof(int))) != cudaSuccess) return bail(e, "cudaMallocHost(flag)");
+    *n->flag_host = 0;
+    float M[kOut * kOut] = {};
     const float sc[kOut] = {10.f, 10.f, 10.f, 6.f, 6.f, 6.f};
-    if ((e = cudaMemcpy(N.scale, sc, sizeof(sc), cudaMemcpyHostToDevice)) != cudaSuccess)
-        return bail(e, "cudaMemcpy(scale)");
+    for (int i = 0; i < kOut; ++i) M[i * kOut + i] = sc[i] * sc[i];
+    if ((e = cudaMemcpy(N.metric, M, sizeof(M), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(e, "cudaMemcpy(metric)");
     *out = n;
     int rc = odo_cnn_init_params(n, 1);
     if (rc != ODO_OK) {
@@ -181,6 +192,9 @@ int odo_cnn_destroy(odo_cnn_t *n) {
     if (n->pack_host) cudaFreeHost(n->pack_host);
     if (n->pack_dev) cudaFree(n->pack_dev);
     if (n->pack_done) cudaEventDestroy(n->pack_done);
+    if (n->done) cudaEventDestroy(n->done);
+    if (n->flag_host) cudaFreeHost(n->flag_host);
+    if (n->in_buf) cudaFree(n->in_buf);
     if (n->own_stream) cudaStreamDestroy(n->own_stream);
     delete n;
     return ODO_OK;
@@ -218,9 +232,12 @@ int odo_cnn_init_params(odo_cnn_t *n, uint64_t seed) {
     return odo_cnn_set_params(n, p.data());
 }
 
-int odo_cnn_set_loss_scale(odo_cnn_t *n, const float scale[6]) {
-    if (!n || !scale) return ODO_ERR_ARG;
-    CCK(cudaMemcpyAsync(n->net.scale, scale, kOut * 4, cudaMemcpyHostToDevice, n->stream));
+int odo_cnn_set_loss_metric(odo_cnn_t *n, const float metric[36]) {
+    if (!n || !metric) return ODO_ERR_ARG;
+    for (int i = 0; i < kOut; ++i)
+        for (int j = 0; j < kOut; ++j)
+            if (!(metric[i * kOut + j] == metric[j * kOut + i])) return ODO_ERR_ARG;  // symmetric, no NaN
+    CCK(cudaMemcpyAsync(n->net.metric, metric, kOut * kOut * 4, cudaMemcpyHostToDevice, n->stream));
     CCK(cudaStreamSynchronize(n->stream));
     return ODO_OK;
 }
@@ -249,6 +266,37 @@ int odo_cnn_pack_input(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t
     CCK(cudaMemcpyAsync(n->pack_dev, n->pack_host, sizeof(PackArgs) * npairs, cudaMemcpyHostToDevice, n->stream));
     CCK(cudaEventRecord(n->pack_done, n->stream));
     CCK(cnn_pack(n->pack_dev, npairs, input_dev, n->stream));
+    return ODO_OK;
+}
+
+int odo_cnn_propose(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_dev) {
+    if (!n || !pairs || !out_dev || npairs < 1) return ODO_ERR_ARG;
+    Net &N = n->net;
+    if (!n->in_buf) CCK(cudaMalloc(&n->in_buf, (size_t)N.max_batch * kInH * kInW * kInC * 2));
+    for (int s = 0; s < npairs; s += N.max_batch) {
+        const int m = npairs - s < N.max_batch ? npairs - s : N.max_batch;
+        int rc = odo_cnn_pack_input(n, pairs + s, m, n->in_buf);
+        if (rc != ODO_OK) return rc;
+        CCK(cnn_forward(N, n->in_buf, m, n->stream));
+        CCK(cudaMemcpyAsync(out_dev + (size_t)6 * s, N.out, (size_t)m * kOut * 4, cudaMemcpyDeviceToDevice,
+                            n->stream));
+    }
+    CCK(cudaMemcpyAsync(n->flag_host, N.err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+    CCK(cudaEventRecord(n->done, n->stream));
+    return ODO_OK;
+}
+
+void *odo_cnn_event(odo_cnn_t *n) { return n ? (void *)n->done : nullptr; }
+
+int odo_cnn_wait(odo_cnn_t *n) {
+    if (!n) return ODO_ERR_ARG;
+    CCK(cudaEventSynchronize(n->done));
+    if (*n->flag_host) {
+        *n->flag_host = 0;
+        n->err = "tensor-core pipeline wait timed out";
+        CCK(cudaMemsetAsync(n->net.err, 0, sizeof(int), n->stream));
+        return ODO_ERR_TIMEOUT;
+    }
     return ODO_OK;
 }
 
@@ -281,7 +329,7 @@ int odo_cnn_train_step(odo_cnn_t *n, const uint16_t *input, const float *labels,
 
 int odo_cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M, int N, int K, int bn, int layout,
                        void *stream) {
-    if (!A || !B || !C || M < 1 || N < 1 || K < 1 || (layout != 0 && layout != 1)) return ODO_ERR_ARG;
+    if (!A || !B || !C || M < 1 || N < 1 || K < 1 || layout < 0 || layout > 2) return ODO_ERR_ARG;
     if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return ODO_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     int *err = nullptr;

@@ -64,6 +64,7 @@ struct Net {
     float *master = nullptr;      // FP32 parameters
     uint16_t *wbf = nullptr;      // BF16 copy (same offsets)
     uint16_t *wt = nullptr;       // BF16 transposed weights (backward data products)
+    uint16_t *wh = nullptr;       // FP16 copy of the first layer's weights (FP16 forward product)
     float *grad = nullptr;        // FP32 gradients (same offsets)
     float *adam_m = nullptr, *adam_v = nullptr;
     uint16_t *act[kConv + 1] = {}; // act[0] unused (input is FP16), act[l] = conv l output
@@ -74,7 +75,7 @@ struct Net {
     uint16_t *dpre[kConv + 1] = {}; // dpre[l]: d loss / d conv l pre-activation (l = 1..6)
     float *dcol = nullptr;        // backward im2col scratch
     float *loss = nullptr;        // device scalar
-    float *scale = nullptr;       // per-output loss scale [6]
+    float *metric = nullptr;      // loss metric, 6x6 row-major
     int *err = nullptr;           // tensor-core wait time-out flag
     int step = 0;
 };

@@ -31,12 +31,13 @@ constexpr int gemm_smem_bytes() {
 
 // `layout` selects the operand core-matrix offsets (0: K-direction 128 B,
 // row-direction 1024 B; 1: the two exchanged) for the layout self-check.
-template <int BN, class LA, class LB, class EP>
+// F16: the loaders return FP16 instead of BF16 values.
+template <int BN, bool F16, class LA, class LB, class EP>
 __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep, int M, int N, int kchunks,
                                                             int chunks_per_split, int layout, int *err) {
     static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "BN");
     constexpr int A_BYTES = 128 * kGemmKChunk * 2, B_BYTES = BN * kGemmKChunk * 2, STAGE = A_BYTES + B_BYTES;
-    constexpr uint32_t IDESC = umma::idesc_bf16_f32(128, BN);
+    constexpr uint32_t IDESC = F16 ? umma::idesc_f16_f32(128, BN) : umma::idesc_bf16_f32(128, BN);
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
 }
 
 // Host-side launch helper (in a .cu translation unit).
-template <int BN, class LA, class LB, class EP>
+template <int BN, class LA, class LB, class EP, bool F16 = false>
 cudaError_t launch_umma_gemm(const LA &la, const LB &lb, const EP &ep, int M, int N, int K, int splits, int layout,
                              int *err, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
@@ -133,13 +134,13 @@ cudaError_t launch_umma_gemm(const LA &la, const LB &lb, const EP &ep, int M, in
     constexpr int smem = gemm_smem_bytes<BN>();
     static bool attr_set = false;  // per instantiation
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN, LA, LB, EP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             smem);
+        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN, F16, LA, LB, EP>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     dim3 grid((M + 127) / 128, (N + BN - 1) / BN, splits);
-    k_umma_gemm<BN, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, per, layout, err);
+    k_umma_gemm<BN, F16, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, per, layout, err);
     return cudaGetLastError();
 }
 

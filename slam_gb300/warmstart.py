@@ -15,7 +15,7 @@ from . import _native
 from .odometry import OdometryError
 
 IN_H, IN_W, IN_C = 120, 160, 8
-DEFAULT_LOSS_SCALE = (10.0, 10.0, 10.0, 6.0, 6.0, 6.0)
+DEFAULT_LOSS_METRIC = np.diag([100.0, 100.0, 100.0, 36.0, 36.0, 36.0])
 
 
 class WarmStartNet:
@@ -67,10 +67,12 @@ class WarmStartNet:
         self._check(self._L.odo_cnn_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
                     "odo_cnn_set_params")
 
-    def set_loss_scale(self, scale):
-        s = np.ascontiguousarray(scale, np.float32).reshape(6)
-        self._check(self._L.odo_cnn_set_loss_scale(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
-                    "odo_cnn_set_loss_scale")
+    def set_loss_metric(self, M):
+        """Loss e^T M e (M symmetric 6x6; e = output - label)."""
+        m = np.ascontiguousarray(M, np.float32).reshape(6, 6)
+        m = np.ascontiguousarray(0.5 * (m + m.T), np.float32)
+        self._check(self._L.odo_cnn_set_loss_metric(self._h, m.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                    "odo_cnn_set_loss_metric")
 
     def _inp(self, x):
         import torch
@@ -94,6 +96,20 @@ class WarmStartNet:
             arr[i] = p.desc()
         self._check(self._L.odo_cnn_pack_input(self._h, arr, n, ctypes.c_void_p(out.data_ptr())),
                     "odo_cnn_pack_input")
+        return out
+
+    def propose(self, frame_pairs, out=None):
+        """Motion proposals [n, 6] (CUDA float32) of FramePairs: packing and
+        forward pass in chunks of max_batch (odo_cnn_propose)."""
+        import torch
+        n = len(frame_pairs)
+        if out is None:
+            out = torch.empty((n, 6), dtype=torch.float32, device="cuda")
+        arr = (_native.OdoPair * n)()
+        for i, p in enumerate(frame_pairs):
+            arr[i] = p.desc()
+        self._check(self._L.odo_cnn_propose(self._h, arr, n, ctypes.c_void_p(out.data_ptr())), "odo_cnn_propose")
+        self._check(self._L.odo_cnn_wait(self._h), "odo_cnn_wait")
         return out
 
     def forward(self, x, out=None):
@@ -259,22 +275,51 @@ def pack_inputs(net, pairset, out=None, chunk=None):
     return out
 
 
-def train(net, inputs, labels, epochs=20, batch=256, lr=1e-3, lr_final=1e-4, seed=0, log=None):
+# label of the horizontally mirrored pair (x -> -x in both cameras)
+MIRROR_SIGN = (-1.0, 1.0, 1.0, 1.0, -1.0, -1.0)
+
+
+def alignment_metric(pairset, sigma=0.01, npairs=64, stride=8):
+    """Loss metric of the point-alignment error: e^T M e = mean squared
+    displacement (in units of sigma) of the scene points p under the motion
+    error e = (dt, dw): d = dt - [p]x dw, M = E[J^T J] / sigma^2 with
+    J = [I, -[p]x], estimated from the model vertices of up to npairs pairs."""
+    n = min(npairs, pairset.n)
+    v = pairset.model_vert[:n, ::stride, ::stride, :].reshape(-1, 4).cpu().numpy().astype(np.float64)
+    p = v[v[:, 3] > 0, :3]
+    mp = p.mean(axis=0)
+    X = np.array([[0, -mp[2], mp[1]], [mp[2], 0, -mp[0]], [-mp[1], mp[0], 0]])
+    M = np.zeros((6, 6))
+    M[:3, :3] = np.eye(3)
+    M[:3, 3:] = -X
+    M[3:, :3] = X
+    M[3:, 3:] = np.mean((p * p).sum(axis=1)) * np.eye(3) - (p.T @ p) / len(p)
+    return M / sigma ** 2
+
+
+def train(net, inputs, labels, epochs=20, batch=256, lr=1e-3, lr_final=1e-4, seed=0, mirror=True, log=None):
     """Adam on shuffled mini-batches (the network's own CUDA kernels);
-    cosine learning-rate decay from lr to lr_final.  Returns the mean loss of
-    every epoch."""
+    cosine learning-rate decay from lr to lr_final; with `mirror`, half of
+    every batch is mirrored horizontally (inputs flipped along x, labels
+    MIRROR_SIGN).  Returns the last batch loss of every epoch."""
     import torch
     n = inputs.shape[0]
     g = torch.Generator(device="cpu").manual_seed(seed)
     steps = epochs * (n // batch)
+    sign = torch.tensor(MIRROR_SIGN, dtype=torch.float32, device="cuda")
     hist, k = [], 0
     for ep in range(epochs):
         perm = torch.randperm(n, generator=g).cuda()
         tot = 0.0
         for s in range(0, n - batch + 1, batch):
             sel = perm[s:s + batch]
-            x = inputs.index_select(0, sel).contiguous()
-            y = labels.index_select(0, sel).contiguous()
+            x = inputs.index_select(0, sel)
+            y = labels.index_select(0, sel)
+            if mirror:
+                h = batch // 2
+                x = torch.cat([x[:h], x[h:].flip(2)])
+                y = torch.cat([y[:h], y[h:] * sign])
+            x, y = x.contiguous(), y.contiguous()
             cur = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * k / max(1, steps)))
             want = (s + 2 * batch > n)
             l = net.train_step(x, y, cur, want_loss=want)
@@ -285,3 +330,105 @@ def train(net, inputs, labels, epochs=20, batch=256, lr=1e-3, lr_final=1e-4, see
         if log:
             log("epoch %d loss %.5f" % (ep, tot))
     return hist
+
+
+def make_training_set(net, batch, seed, n, chunk=2048, max_deg=10.0, max_m=0.10, cam=None, agree_deg=0.5,
+                      agree_m=0.02, log=None):
+    """n seeded room pairs rendered on the GPU in chunks, labelled by the
+    plain tracker and packed into network inputs; only the pairs where the
+    plain tracker converged (within agree_deg / agree_m of the rendering pose)
+    are kept.  Returns a dict: 'inputs' [m,120,160,8] float16 and 'labels'
+    [m,6] float32 (CUDA), 'residuals' (plain tracker, kept pairs), 'kept'
+    (fraction), 'metric' (alignment_metric of the first chunk)."""
+    import torch
+    from . import synth
+    cam = cam or synth.Camera()
+    xs, ys, res, kept, metric = [], [], [], 0, None
+    for c, s in enumerate(range(0, n, chunk)):
+        m = min(chunk, n - s)
+        ps = make_room_pairs(seed * 1000003 + c, m, cam, max_deg, max_m)
+        if metric is None:
+            metric = alignment_metric(ps)
+        lab, ok, err = _label_with_residual(batch, ps, agree_deg=agree_deg, agree_m=agree_m)
+        X = pack_inputs(net, ps)
+        sel = torch.from_numpy(np.nonzero(ok)[0]).cuda()
+        xs.append(X.index_select(0, sel))
+        ys.append(torch.from_numpy(lab[ok]).cuda())
+        res.append(err[ok])
+        kept += int(ok.sum())
+        del ps, X
+        if log:
+            log("training chunk %d: %d pairs, %d kept" % (c, m, int(ok.sum())))
+    return {"inputs": torch.cat(xs), "labels": torch.cat(ys), "residuals": np.concatenate(res),
+            "kept": kept / max(n, 1), "metric": metric}
+
+
+def _label_with_residual(batch, pairset, chunk=512, agree_deg=0.5, agree_m=0.02):
+    from .batch import result_pose
+    from .synth import pose_error
+    labels = np.zeros((pairset.n, 6), np.float32)
+    ok = np.zeros(pairset.n, bool)
+    err = np.zeros(pairset.n, np.float32)
+    for s in range(0, pairset.n, chunk):
+        idx = list(range(s, min(pairset.n, s + chunk)))
+        res = track_plain(batch, pairset, idx)
+        for i, r in zip(idx, res):
+            T = result_pose(r)
+            labels[i] = motion_vec(np.linalg.inv(pairset.T1[i]) @ T)
+            e = pose_error(T, pairset.T2[i])
+            ok[i] = e[0] <= np.radians(agree_deg) and e[1] <= agree_m
+            err[i] = r.lastICPError
+    return labels, ok, err
+
+
+class WarmStartTracker:
+    """Batched tracking started from the network's motion proposal, with a
+    fallback to the plain tracker.
+
+    Per batch: network inputs from the level-0 frames (block means to
+    160x120), forward pass, tracking from pose * exp(proposal) with a short
+    schedule (`levels`, `iterations`, no SO3 stage).  A pair falls back to the
+    plain tracker (SO3 + the reference's 10/5/4 schedule) when its final ICP
+    residual exceeds `residual_ratio` x the plain tracker's typical residual
+    (`plain_residual`, the median over the training pairs) or when the refined
+    pose differs from the proposal by more than `max_disagree_deg`."""
+
+    def __init__(self, net, batch, plain_residual, levels=2, iterations=(4, 3, 0), residual_ratio=1.5,
+                 max_disagree_deg=0.5, max_pairs=512):
+        import torch
+        self.net, self.batch = net, batch
+        self.plain_residual = float(plain_residual)
+        self.levels, self.iterations = int(levels), tuple(iterations)
+        self.residual_ratio, self.max_disagree = float(residual_ratio), np.radians(max_disagree_deg)
+        self.inputs = torch.empty((max_pairs, IN_H, IN_W, IN_C), dtype=torch.float16, device="cuda")
+        self.props = torch.empty((max_pairs, 6), dtype=torch.float32, device="cuda")
+
+    def track(self, frame_pairs):
+        """Returns (results, fallback mask, proposals [n,6])."""
+        from .batch import result_pose
+        from .synth import pose_error
+        n = len(frame_pairs)
+        for s in range(0, n, self.net.max_batch):
+            e = min(n, s + self.net.max_batch)
+            self.net.pack(frame_pairs[s:e], self.inputs[s:e])
+            self.net.forward(self.inputs[s:e], out=self.props[s:e])
+        short = [_with_schedule(p, self.levels, self.iterations) for p in frame_pairs]
+        res = list(self.batch.track_init(short, self.props[:n]))
+        prop = self.props[:n].cpu().numpy().astype(np.float64)
+        fb = np.zeros(n, bool)
+        for i, r in enumerate(res):
+            T0 = np.asarray(frame_pairs[i].pose, np.float64) @ vec_motion(prop[i])
+            dis = pose_error(result_pose(r), T0)[0]
+            fb[i] = (r.lastICPError > self.residual_ratio * self.plain_residual) or dis > self.max_disagree
+        if fb.any():
+            idx = np.nonzero(fb)[0]
+            plain = self.batch.track([frame_pairs[i] for i in idx])
+            for k, i in enumerate(idx):
+                res[i] = plain[k]
+        return res, fb, prop
+
+
+def _with_schedule(p, levels, iterations):
+    from .batch import FramePair
+    return FramePair(p.cam, p.model_vert, p.model_norm, p.model_rgba, p.depth, p.rgba, p.prev_rgba, p.pose,
+                     levels=levels, iterations=iterations)

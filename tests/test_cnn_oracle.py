@@ -38,7 +38,8 @@ def test_oracle_backward_against_finite_differences(orc):
     xi = x.view(np.uint16)
     p, w, b = _params(orc, rng)
     lab = rng.normal(0, 0.05, (B, 6))
-    sc = np.array([10, 10, 10, 6, 6, 6.0])
+    A = rng.normal(size=(6, 6))
+    sc = A @ A.T + np.eye(6)
     _, _, g = orc.cnn_run(p, xi, lab, sc, rounding=False)
     # a non-zero-channel weight of every layer and every bias
     idx = [w[0] + 2, w[1] + 20, w[2] + 77, w[3] + 301, w[4] + 999, w[5] + 5, w[6] + 4242, w[7] + 100,

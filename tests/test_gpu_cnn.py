@@ -36,6 +36,20 @@ def test_umma_gemm_matches_torch(gpu, bn, shape):
     assert err <= tol, (bn, shape, err, tol)
 
 
+@pytest.mark.parametrize("bn", [32, 128])
+def test_umma_gemm_fp16_operands(gpu, bn):
+    """The FP16 variant (first network layer): against torch on FP16 values."""
+    import torch
+    from slam_gb300.warmstart import debug_gemm
+    g = torch.Generator(device="cuda").manual_seed(bn)
+    A = torch.randn(200, 72, device="cuda", generator=g).half()
+    B = torch.randn(32, 72, device="cuda", generator=g).half()
+    ref = A.float() @ B.float().T
+    C = debug_gemm(A.view(torch.bfloat16), B.view(torch.bfloat16), bn=bn, layout=2)
+    torch.cuda.synchronize()
+    assert (C - ref).abs().max().item() <= 1e-4 * ref.abs().max().item() + 1e-4
+
+
 def test_umma_operand_layout_self_check(gpu):
     """The exchanged core-matrix offsets give a different (wrong) product:
     the layout test above is sensitive to the descriptor's offsets."""
@@ -72,12 +86,12 @@ def _net_and_inputs(B, seed):
 
 def test_cnn_forward_matches_oracle(gpu, orc):
     import torch
-    from slam_gb300.warmstart import DEFAULT_LOSS_SCALE
+    from slam_gb300.warmstart import DEFAULT_LOSS_METRIC
     net, x, lab, xd, ld = _net_and_inputs(3, 11)
     out = net.forward(xd)
     torch.cuda.synchronize()
     p = net.get_params()
-    o_ref, loss_ref, _ = orc.cnn_run(p, x.view(np.uint16), lab, DEFAULT_LOSS_SCALE, rounding=True, want_grad=False)
+    o_ref, loss_ref, _ = orc.cnn_run(p, x.view(np.uint16), lab, DEFAULT_LOSS_METRIC, rounding=True, want_grad=False)
     o = out.cpu().numpy().astype(np.float64)
     # The tensor cores accumulate in FP32 in their own order; where a sum lies
     # within that difference of a BF16 rounding boundary the stored activation
@@ -85,18 +99,24 @@ def test_cnn_forward_matches_oracle(gpu, orc):
     # remaining layers: agreement to ~1e-3 of the output scale, not bitwise.
     rel = np.abs(o - o_ref).max() / np.abs(o_ref).max()
     assert rel < 1e-2, rel
-    assert abs(loss_ref - float(np.sum((np.asarray(DEFAULT_LOSS_SCALE) * (o - lab)) ** 2) / 3)) < 1e-2 * loss_ref
+    e = o - lab
+    assert abs(loss_ref - float(np.einsum("bi,ij,bj->", e, DEFAULT_LOSS_METRIC, e)) / 3) < 1e-2 * loss_ref
 
 
 def test_cnn_gradients_match_oracle(gpu, orc):
     """Per layer, the GPU's weight and bias gradients (tensor-core products,
     FP32 accumulation) against the CPU oracle with the same BF16 rounding
-    points: relative error of each gradient tensor."""
-    from slam_gb300.warmstart import DEFAULT_LOSS_SCALE
+    points: relative error of each gradient tensor.  A full (non-diagonal)
+    loss metric."""
     net, x, lab, xd, ld = _net_and_inputs(2, 23)
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(6, 6))
+    metric = A @ A.T + np.eye(6)
+    net.set_loss_metric(metric)
+    metric = metric.astype(np.float32).astype(np.float64)
     g, loss = net.gradients(xd, ld)
     p = net.get_params()
-    _, loss_ref, g_ref = orc.cnn_run(p, x.view(np.uint16), lab, DEFAULT_LOSS_SCALE, rounding=True)
+    _, loss_ref, g_ref = orc.cnn_run(p, x.view(np.uint16), lab, metric, rounding=True)
     assert abs(loss - loss_ref) <= 1e-3 * abs(loss_ref)
     w, b, total = orc.cnn_layout()
     rows = [32, 64, 128, 128, 128, 128, 768, 6]
@@ -104,8 +124,11 @@ def test_cnn_gradients_match_oracle(gpu, orc):
     for l in range(8):
         for name, off, n in (("W", w[l], rows[l] * cols[l]), ("b", b[l], rows[l])):
             a, r = g[off:off + n].astype(np.float64), g_ref[off:off + n]
+            # gradients are sums with heavy cancellation: the FP32 order of the
+            # tensor cores moves BF16 rounding decisions of the activation
+            # gradients (one BF16 ulp = 2^-8), hence a 1 % bound
             rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
-            assert rel < 5e-3, (l, name, rel)
+            assert rel < 1e-2, (l, name, rel)
 
 
 def test_cnn_training_reduces_loss(gpu):
