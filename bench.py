@@ -57,8 +57,11 @@ def parse():
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
+    ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
+                    help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
     ap.add_argument("--train-pairs", type=int, default=50000, help="warm study: rendered training pairs")
     ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-pairs", type=int, default=2000)
     ap.add_argument("--warm-levels", type=int, default=3)
     ap.add_argument("--warm-iters", default="6,4,4")
@@ -352,13 +355,13 @@ def run_ours(args):
     return out
 
 
-def make_batch_pairs(n, seed):
+def make_batch_pairs(n, seed, sizes="mixed"):
     """Mixed-resolution verification pairs: sizes uniform over
-    {160x120, 320x240, 640x480} (fx scaled), seeded rooms, motion <= 8 deg /
-    15 cm, 2-3 pyramid levels."""
+    {160x120, 320x240, 640x480} (fx scaled; or 640x480 only), seeded rooms,
+    motion <= 8 deg / 15 cm, 2-3 pyramid levels."""
     from slam_gb300 import synth
     rng = np.random.default_rng(seed)
-    sizes = [(160, 120), (320, 240), (640, 480)]
+    sizes = [(160, 120), (320, 240), (640, 480)] if sizes == "mixed" else [(640, 480)] * 3
     rooms = [synth.make_room(seed * 1000 + r, 20) for r in range(16)]
     pairs = []
     for i in range(n):
@@ -376,7 +379,7 @@ def run_batch_study(args):
     from slam_gb300.batch import BatchOdometry, FramePair, result_pose
     torch.cuda.set_device(0)
     t0 = time.time()
-    pairs = make_batch_pairs(args.pairs, args.seed)
+    pairs = make_batch_pairs(args.pairs, args.seed, args.sizes)
     gen_s = time.time() - t0
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     devd = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int16)).cuda().view(torch.uint16)
@@ -420,8 +423,9 @@ def run_batch_study(args):
     out = {"metric": "batched verification pairs/s (mixed 160x120-640x480, one CUDA graph)",
            "value": len(pairs) / (ms * 1e-3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "data": "synthetic",
-           "config": {"workload": f"{len(pairs)} pairs per launch, sizes uniform over 160x120/320x240/640x480, "
-                                  "motion <= 8 deg / 15 cm, 2-3 levels, ICP+RGB, SO3 on",
+           "config": {"workload": f"{len(pairs)} pairs per launch, sizes " +
+                                  ("uniform over 160x120/320x240/640x480" if args.sizes == "mixed" else "640x480") +
+                                  ", motion <= 8 deg / 15 cm, 2-3 levels, ICP+RGB, SO3 on",
                       "autotuned_launch": {"threads": threads, "pixels_per_thread": ppt, "ms": tune_ms},
                       "default_launch": {"threads": 256, "pixels_per_thread": 2, "ms_host_timed": default_ms},
                       "generation_s": gen_s},
@@ -626,7 +630,8 @@ def run_warm_study(args):
         gen_s = time.time() - t0
         net.set_loss_metric(ts["metric"])
         t0 = time.time()
-        hist = ws.train(net, ts["inputs"], ts["labels"], epochs=args.epochs, batch=256, lr=1e-3, lr_final=3e-5)
+        hist = ws.train(net, ts["inputs"], ts["labels"], epochs=args.epochs, batch=256, lr=args.lr,
+                        lr_final=args.lr / 30)
         torch.cuda.synchronize()
         train_s = time.time() - t0
         plain_res = float(np.median(ts["residuals"]))

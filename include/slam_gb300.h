@@ -299,7 +299,9 @@ int odo_icp_step_noalloc(const float *vmap_curr, const float *nmap_curr, const f
  * frames' 160x120 depth and gray images; forward and backward products run
  * on the tcgen05 tensor cores (FP32 accumulation).
  * Input [B][120][160][8] FP16 NHWC: model depth (m), model gray (0..1), live
- * depth (m), live gray, four zero channels.  Output [B][6]: translation (m)
+ * depth (m), live gray, and four channels derived from them: live - model
+ * gray, live - model depth, valid-depth fractions of the model and live
+ * blocks.  Output [B][6]: translation (m)
  * and rotation vector (rad) of the live camera in the model camera's frame.
  * Six 3x3/stride-2 convolutions (8->32->64->128->128->128->128, ReLU; the
  * first one with FP16 operands, the others BF16), fc
@@ -319,8 +321,8 @@ int odo_cnn_set_loss_metric(odo_cnn_t *n, const float metric[36]); /* row-major,
 int odo_cnn_forward(odo_cnn_t *n, const uint16_t *input_dev, int batch, float *out_dev);
 /* Network inputs [npairs][120][160][8] of frame pairs whose level-0 size is
  * (160 s) x (120 s): s x s block means of the model depth (vertex z) and
- * intensity and of the live depth and intensity (asynchronous, on the
- * network's stream). */
+ * intensity and of the live depth and intensity, and the derived channels
+ * (asynchronous, on the network's stream). */
 int odo_cnn_pack_input(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t *input_dev);
 /* Motion proposals [npairs][6] (device) of frame pairs whose level-0 size is
  * (160 s) x (120 s): packing and forward pass in chunks of the network's

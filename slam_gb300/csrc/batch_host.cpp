@@ -319,6 +319,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
         std::memcpy(at(b->o_so3) + i * sizeof(So3Args), &so, sizeof(so));
         // iteration schedule (src/odom/RGBDOdometryef.cpp:382-384), restricted to `levels`
         const int base[kLevels] = {fastOdom ? 3 : 10, 5, 4};
+        int sched[kLevels];
         for (int l = 0; l < kLevels; ++l) {
             PassArgs a{};
             LevelArgs &L = a.L;
@@ -346,6 +347,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             a.st = b->st_dev + i;
             a.ws = p.ws;
             a.iters = (l < q.levels) ? (q.iterations[l] > 0 ? q.iterations[l] : base[l]) : 0;
+            sched[l] = a.iters;
             const int npx = L.cols * L.rows;
             a.nb_icp = a.iters ? blocks_for(b, npx) : 0;
             a.nb_rgb = a.iters ? (rgb ? a.nb_icp : 1) : 0;
@@ -369,6 +371,14 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
         st.so3 = so3 ? 1 : 0;
         for (int k = 0; k < 9; ++k) st.resultR[k] = (k % 4 == 0) ? 1.0 : 0.0;
         st.lastICPCount = st.lastRGBCount = st.lastSO3Count = (float)(p.w * p.h);
+        for (int l = 0; l < kLevels; ++l) {
+            const Intr K = intr(l);
+            st.Kl[l][0] = K.fx;
+            st.Kl[l][1] = K.fy;
+            st.Kl[l][2] = K.cx;
+            st.Kl[l][3] = K.cy;
+            st.sched[l] = sched[l];
+        }
     }
 }
 

@@ -327,7 +327,10 @@ __global__ void k_transpose_bf16(const uint16_t *w, int rows, int cols, uint16_t
 
 // Network input of pair blockIdx.z: s x s block means of the valid depths
 // (metres; 0 where no pixel is valid) and of the intensities (the tracker's
-// weighting of the RGBA bytes, 0..1), FP16, four zero channels.
+// weighting of the RGBA bytes, 0..1) of both frames, FP16; channels 4-7 are
+// derived from them in FP32 before rounding: live - model intensity, live -
+// model depth (0 unless both are valid), and the valid-depth fractions of the
+// two blocks (the differences keep the precision that FP16 depth loses).
 __global__ void k_pack(const PackArgs *args, uint16_t *out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= kInW || y >= kInH) return;
@@ -360,13 +363,17 @@ __global__ void k_pack(const PackArgs *args, uint16_t *out) {
             lg += (float)e.x * 0.114f + (float)e.y * 0.299f + (float)e.z * 0.587f;
         }
     }
-    const float inv = 1.f / (255.f * a.s * a.s);
+    const float inv = 1.f / (255.f * a.s * a.s), invn = 1.f / (a.s * a.s);
+    const float dm = nm ? md / nm : 0.f, dl = nl ? ld / nl : 0.f, gm = mg * inv, gl = lg * inv;
     __align__(16) __half h[8];
-    h[0] = __float2half_rn(nm ? md / nm : 0.f);
-    h[1] = __float2half_rn(mg * inv);
-    h[2] = __float2half_rn(nl ? ld / nl : 0.f);
-    h[3] = __float2half_rn(lg * inv);
-    h[4] = h[5] = h[6] = h[7] = __float2half_rn(0.f);
+    h[0] = __float2half_rn(dm);
+    h[1] = __float2half_rn(gm);
+    h[2] = __float2half_rn(dl);
+    h[3] = __float2half_rn(gl);
+    h[4] = __float2half_rn(gl - gm);
+    h[5] = __float2half_rn((nm && nl) ? dl - dm : 0.f);
+    h[6] = __float2half_rn(nm * invn);
+    h[7] = __float2half_rn(nl * invn);
     uint16_t *o = out + (((size_t)blockIdx.z * kInH + y) * kInW + x) * kInC;
     *reinterpret_cast<uint4 *>(o) = *reinterpret_cast<const uint4 *>(h);
 }

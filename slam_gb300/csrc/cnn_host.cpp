@@ -78,14 +78,12 @@ void he_init(const ParamLayout &L, uint64_t seed, std::vector<float> &p) {
     };
     for (int l = 0; l < kLayers; ++l) {
         const int rows = w_rows(l), cols = w_cols(l);
-        // conv1: only the 4 real input channels of each tap count as fan-in
-        const double fan_in = l == 0 ? 9.0 * 4.0 : (double)cols;
+        const double fan_in = (double)cols;
         const double sd = (l == kLayers - 1) ? 0.1 * std::sqrt(1.0 / fan_in) : std::sqrt(2.0 / fan_in);
         for (int r = 0; r < rows; ++r)
             for (int c = 0; c < cols; ++c) {
                 const double u1 = next(), u2 = next();
-                double v = sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
-                if (l == 0 && (c % kCin[0]) >= 4) v = 0.0;  // zero input channels
+                const double v = sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
                 p[L.w[l] + (size_t)r * cols + c] = (float)v;
             }
     }

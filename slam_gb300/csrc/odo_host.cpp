@@ -488,6 +488,14 @@ int odo_get_incremental_transformation(odo_t *h, float trans[3], float rot[9], i
     st->rgb = rgb;
     st->so3 = so3 ? 1 : 0;
     st->status = 0;
+    for (int l = 0; l < kLevels; ++l) {
+        const Intr K = level_args(h, l).K;
+        st->Kl[l][0] = K.fx;
+        st->Kl[l][1] = K.fy;
+        st->Kl[l][2] = K.cx;
+        st->Kl[l][3] = K.cy;
+        st->sched[l] = iterations[l];
+    }
     if (h->mode == ODO_MODE_GRAPH) {
         GraphKey key{icp, rgb, so3 ? 1 : 0, iterations[0], iterations[1], iterations[2], h->parity, h->precision};
         auto it = h->graphs.find(key);

@@ -49,6 +49,12 @@ struct TrackState {
     double resultR[9];   // SO3 pre-alignment result
     float Rcurr[9], tcurr[3];
     float krkinv[9], kt[3];  // photometric warp of the next iteration (same level)
+    // photometric warp of the first iteration of each level (computed from
+    // resultRt when the previous level ends), the levels' intrinsics
+    // (fx, fy, cx, cy) and the iterations scheduled per level
+    float krk0[kLevels][9], kt0[kLevels][3];
+    float Kl[kLevels][4];
+    int sched[kLevels];
     float sigmaVal;
     int level_break;     // rgbOnly early exit for the current level
     // statistics (RGBDOdometryef public members)

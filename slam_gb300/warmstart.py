@@ -4,8 +4,9 @@ reference).
 A BF16 CNN proposes the SE(3) motion of a frame pair from both frames'
 160x120 depth and gray images; its forward and backward products run on the
 library's tcgen05 GEMM.  Inputs are CUDA tensors: [B, 120, 160, 8] float16
-(model depth m, model gray, live depth m, live gray, four zeros); outputs
-[B, 6] float32 (translation m, rotation vector rad).
+(model depth m, model gray, live depth m, live gray, live - model gray, live
+- model depth, valid-depth fractions of both frames); outputs [B, 6] float32
+(translation m, rotation vector rad).
 """
 import ctypes
 
@@ -275,7 +276,8 @@ def pack_inputs(net, pairset, out=None, chunk=None):
     return out
 
 
-# label of the horizontally mirrored pair (x -> -x in both cameras)
+# label of the horizontally mirrored pair (x -> -x in both cameras); the
+# input channels are all mirror-invariant images
 MIRROR_SIGN = (-1.0, 1.0, 1.0, 1.0, -1.0, -1.0)
 
 
