@@ -1,24 +1,31 @@
-"""Benchmark of the dense RGB-D tracking step (frames/s at 640x480).
+"""Benchmark of the dense RGB-D tracking step (frames/s at 640x480):
+warm-started batched tracking against the plain tracker.
 
-A step = one frame of frame-to-model tracking through the public API, in the
-reference's call order: initICPModel (model vertices/normals, RGBA32F) ->
-initRGBModel -> initICP (uint16 depth) -> initRGB -> getIncrementalTransformation
-(3 pyramid levels, 10/5/4 ICP+RGB iterations, icpWeight 10, SO3 on).
-
-Workload: the synthetic 300-frame Catmull-Rom trajectory through the 6x4x3 m
-room with 20 spheres (<= 1.5 deg / 3 cm per frame), fx = fy = 525,
-cx = 319.5, cy = 239.5, depth noise 0.0012 z^2, 5 % dropout; the model
-prediction is ray-cast noise-free at the previous ground-truth pose.  A pool of
-the first P frames (default 64, ~13 MB of inputs each, > L2 in total) is
-resident in HBM and cycled, so every step reads its inputs from HBM.
+Headline (value): warm-started batched tracking.  A step = one batch of
+--batch-pairs held-out 640x480 frame pairs (6x4x3 m rooms with 20 spheres,
+fx = fy = 525, depth noise 0.0012 z^2, 5 % dropout, relative motion <= 10 deg /
+10 cm) tracked by one odo_batch_track_warm call: the warm-start network's
+proposal for every pair, 3 pyramid levels with 6/4/4 ICP+RGB iterations and
+no SO3 stage, and a fall-back to the reference's schedule (SO3 + 10/5/4) for
+the pairs whose residual or proposal disagreement fails the test.  The
+network is trained first, on the GPU, by the library's own kernels, on
+GPU-rendered pairs labelled by the plain tracker (setup, not timed).  Two
+batches (> L2) are resident in HBM and alternate.  Beside it, on the same
+pairs: the plain batched tracker (odo_batch_track), and the plain
+single-pair drop-in path (one frame per call through the reference's call
+order initICPModel -> initRGBModel -> initICP -> initRGB ->
+getIncrementalTransformation, on the 300-frame synthetic trajectory).
 
 Arms:
-  ours (default)  the CUDA library; value = frames/s with inputs in HBM,
-                  e2e = frames/s with inputs in pinned host memory copied per
-                  step (and the pose/statistics read back);
-  --impl reference  the reference's tracking math on the host cores (the CPU
-                  oracle, a restatement of src/odom/*; the reference itself
-                  cannot be built here), all host threads.
+  ours (default)  the CUDA library; value = warm-started frames/s with inputs
+                  in HBM; e2e = the same with every step's inputs copied from
+                  pinned host memory and the results read back;
+  --impl reference  the reference's tracking math (plain schedule) on the host
+                  cores (the CPU oracle, a restatement of src/odom/*; the
+                  reference itself cannot be built here), all host threads, on
+                  pairs of the same distribution.
+Studies (--study): batch (mixed-resolution verification), precision
+(corridor pairs against the FP64 oracle), warm (the warm start in detail).
 Multi-GPU: replicas (a tracking call does not shard); each rank tracks its own
 copy of the workload; value = frames of all ranks / max time over ranks.
 """
@@ -38,6 +45,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ICP+RGB tracking frames/s @640x480: warm-started vs plain, equal pose error"
 BYTES_PER_PX_ITER = 62  # ICP 48 B (4 maps x 12 B) + photometric 14 B per pixel-iteration
+# the association/residual kernel's share: ICP 48 B + nextImage 1 + nextDepth 4
+# + lastDepth 4 + lastImage 1 (the derivative images, 4 B, are read by the
+# photometric/solve kernel)
+PASS1_BYTES_PER_PX = 58
 PREPROC_BYTES_PER_PX = 140  # per-frame map/pyramid building, per level-0 pixel (x 4/3 over the pyramid)
 
 
@@ -57,6 +68,7 @@ def parse():
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
+    ap.add_argument("--no-prefetch", action="store_true", help="disable the iteration kernels' L2 bulk prefetch")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
     ap.add_argument("--train-pairs", type=int, default=50000, help="warm study: rendered training pairs")
@@ -70,6 +82,9 @@ def parse():
     ap.add_argument("--save-params", default=None)
     ap.add_argument("--load-params", default=None, help="warm study: skip training, use these parameters")
     ap.add_argument("--sweep", action="store_true", help="warm study: also evaluate other warm schedules")
+    ap.add_argument("--batch-pairs", type=int, default=500, help="pairs per warm-started batched step")
+    ap.add_argument("--batch-steps", type=int, default=6, help="timed warm-started batched steps")
+    ap.add_argument("--residual-ratio", type=float, default=1.5)
     a = ap.parse_args()
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
@@ -197,17 +212,20 @@ def run_reference(args):
     from oracle import oracle
     ncores = os.cpu_count() or 1
     oracle.set_threads(ncores)
-    cam, frames = make_pool(min(args.pool, 8), args.seed)
+    from slam_gb300 import synth
+    cam = synth.Camera()
+    frames = [synth.make_pair(args.seed * 31 + 7000 + k, cam=cam, max_deg=10.0, max_m=0.10) for k in range(8)]
     cpu_track(frames, cam, nframes=max(1, args.warmup))
     n, el = cpu_track(frames, cam, nframes=args.steps)
     fps = n / el
     out = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / n, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "640x480 frame-to-model tracking, 300-frame synthetic room trajectory",
+           "config": {"workload": "640x480 room pairs (6x4x3 m rooms, 20 spheres, motion <= 10 deg / 10 cm), "
+                                  "plain tracking (the reference has no warm start)",
                       "iterations": [10, 5, 4], "icpWeight": 10, "so3": True},
            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": oracle.get_threads(), "kind": "port",
-                            "sample": f"{n} frames of the trajectory on the host cores"},
+                            "sample": f"{n} pair trackings (8 distinct pairs cycled) on the host cores"},
            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -304,7 +322,7 @@ def run_ours(args):
     k_ms, s_ms, it_ms = odo.time_iteration(0, reps=100)
     level_ms["L0"] = [k_ms, s_ms, it_ms]
     n0 = cam.width * cam.height
-    alg_bytes = BYTES_PER_PX_ITER * n0
+    alg_bytes = PASS1_BYTES_PER_PX * n0
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     launches_per_frame = 10 + 4 + 2 * (10 + 5 + 4)
@@ -325,34 +343,194 @@ def run_ours(args):
             cpu = {"value": None, "unit": "frames/s", "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
         rot = [e[0] for e in errs]
         tr = [e[1] for e in errs]
-        out = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
-               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        plain = {"frames_per_s": fps, "ms_per_frame": ms / args.steps, "steps": args.steps,
+                 "workload": "640x480 frame-to-model tracking, one frame per call (the drop-in path), synthetic "
+                             f"300-frame room trajectory, first {len(frames)} frames cycled",
+                 "levels": ["640x480", "320x240", "160x120"], "iterations": [10, 5, 4], "icpWeight": 10,
+                 "so3": True, "mode": args.mode,
+                 "l2": f"inputs larger than L2: {len(frames)} frames x {in_bytes / 1e6:.1f} MB resident in HBM, "
+                       "a different frame every step",
+                 "e2e": {"value": fps_e2e, "unit": "frames/s", "h2d_bytes_per_step": int(in_bytes),
+                         "d2h_bytes_per_step": int(_native.load().odo_state_bytes())},
+                 "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres (level 0)", "achieved": achieved,
+                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                              "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
+                              "alg_bytes_per_launch": alg_bytes,
+                              "note": "level-0 maps (~20 MB) are L2-resident within a frame"},
+                 "frame_bytes": frame_bytes(cam, iters[1:]),
+                 "frame_roofline_gbs": frame_bytes(cam, iters[1:]) / (ms / args.steps * 1e-3) / 1e9,
+                 "pose_error_vs_gt": {"rot_rad_mean": float(np.mean(rot)), "trans_m_mean": float(np.mean(tr)),
+                                      "rot_rad_max": float(np.max(rot)), "trans_m_max": float(np.max(tr))},
+                 "iterations": iters, "clocks": clk, "iteration_ms_by_level": level_ms,
+                 "device_phases_us": phases, "gpu_launches": launches_per_frame * args.steps}
+    warm = measure_warm_batched(args, stream, local, world)
+    if rank == 0:
+        W = warm
+        out = {"metric": METRIC, "value": W["fps"], "unit": "frames/s", "n_gpus": world, "steps": W["steps"],
+               "warmup": W["warmup"], "ms_per_step": W["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-               "config": {"workload": "640x480 frame-to-model tracking (plain path), synthetic 300-frame room "
-                                      f"trajectory, first {len(frames)} frames cycled",
-                          "levels": ["640x480", "320x240", "160x120"], "iterations": [10, 5, 4],
-                          "icpWeight": 10, "so3": True, "mode": args.mode,
-                          "l2": f"inputs larger than L2: {len(frames)} frames x {in_bytes / 1e6:.1f} MB resident "
-                                "in HBM, a different frame every step",
+               "config": {"workload": f"warm-started batched tracking: {W['batch_pairs']} held-out 640x480 room pairs "
+                                      "per step (6x4x3 m rooms, 20 spheres, motion <= 10 deg / 10 cm), network "
+                                      "proposal + 3 levels 6/4/4 without SO3, fall-back to the plain schedule",
+                          "batch_pairs": W["batch_pairs"], "warm_schedule": W["schedule"],
+                          "fallback": W["fallback_cfg"], "train": W["train"], "launch": W["launch"],
+                          "l2": f"inputs larger than L2: {W['pool_batches']} batches x {W['batch_bytes'] / 1e9:.1f} GB "
+                                "resident in HBM, alternating",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
-               "e2e": {"value": fps_e2e, "unit": "frames/s", "h2d_bytes_per_step": int(in_bytes),
-                       "d2h_bytes_per_step": int(_native.load().odo_state_bytes())},
-               "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres (level 0)", "achieved": achieved,
-                            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                            "traffic": None, "kernel_ms": k_ms, "photometric_kernel_ms": s_ms,
-                            "iteration_ms": it_ms, "alg_bytes_per_launch": alg_bytes,
-                            "note": "level-0 maps (~20 MB) are L2-resident within a frame"},
-               "frame_bytes": frame_bytes(cam, iters[1:]),
-               "frame_roofline_gbs": frame_bytes(cam, iters[1:]) / (ms / args.steps * 1e-3) / 1e9,
-               "pose_error_vs_gt": {"rot_rad_mean": float(np.mean(rot)), "trans_m_mean": float(np.mean(tr)),
-                                    "rot_rad_max": float(np.max(rot)), "trans_m_max": float(np.max(tr))},
-               "iterations": iters, "clocks": clk,
-               "iteration_ms_by_level": level_ms, "device_phases_us": phases, "gpu_launches": launches_per_frame * args.steps,
-               "cpu_baseline": cpu}
+               "e2e": W["e2e"], "roofline": W["roofline"],
+               "plain_batched": W["plain_batched"], "plain_single_pair": plain,
+               "speedup": {"vs_plain_single_pair": W["fps"] / plain["frames_per_s"],
+                           "vs_plain_batched": W["fps"] / W["plain_batched"]["frames_per_s"]},
+               "pose_error_vs_gt": W["pose_error_vs_gt"], "fallback_rate": W["fallback_rate"],
+               "iterations_mean": W["iterations_mean"], "clocks": W["clocks"],
+               "gpu_launches": W["gpu_launches"], "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return out
+
+
+def measure_warm_batched(args, stream, local, world):
+    """The headline: warm-started batched tracking of 640x480 pairs (the
+    network trained here first, on the GPU, by the library's own kernels),
+    with the plain batched tracker timed on the same pairs."""
+    import torch
+    from slam_gb300 import synth, warmstart as ws
+    from slam_gb300.batch import BatchOdometry
+    cam = synth.Camera()
+    nb = args.batch_pairs
+    b = BatchOdometry(nb, stream=stream.cuda_stream)
+    net = ws.WarmStartNet(max_batch=256, stream=stream.cuda_stream)
+    t0 = time.time()
+    ts = ws.make_training_set(net, b, args.seed * 17 + 3, args.train_pairs)
+    net.set_loss_metric(ts["metric"])
+    gen_s = time.time() - t0
+    t0 = time.time()
+    hist = ws.train(net, ts["inputs"], ts["labels"], epochs=args.epochs, batch=256, lr=args.lr, lr_final=args.lr / 30)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    plain_res = float(np.median(ts["residuals"]))
+    n_train = int(ts["labels"].shape[0])
+    del ts
+    its = tuple(int(v) for v in args.warm_iters.split(","))
+    wkw = dict(levels=args.warm_levels, iterations=its, residual_limit=args.residual_ratio * plain_res,
+               max_disagree_deg=args.max_disagree)
+    pool = [ws.make_room_pairs(args.seed * 31 + 1000 + k, nb, cam, 10.0, 0.10) for k in range(2)]
+    fps = [p.frame_pairs() for p in pool]
+    descs = [b._descs(f) for f in fps]
+    batch_bytes = sum(t[0].numel() * t[0].element_size() * nb for t in
+                      (pool[0].model_vert, pool[0].model_norm, pool[0].model_rgba, pool[0].depth, pool[0].rgba))
+    threads, ppt, _ = b.autotune(fps[0])
+    W = max(args.warmup, 3)
+    K = args.batch_steps
+    for k in range(W):
+        b.track(fps[k % 2], descs=descs[k % 2])
+        b.track_warm(net, fps[k % 2], descs=descs[k % 2], **wkw)
+    # ---- warm-started, inputs resident in HBM ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res_w, fb_all = [], []
+    e0.record(stream)
+    for k in range(K):
+        r, fb = b.track_warm(net, fps[k % 2], descs=descs[k % 2], **wkw)
+        res_w.append(r)
+        fb_all.append(fb)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_w = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    # ---- plain batched on the same pairs ----
+    torch.cuda.synchronize()
+    res_p = []
+    e0.record(stream)
+    for k in range(K):
+        res_p.append(b.track(fps[k % 2], descs=descs[k % 2]))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_p = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([ms_w, ms_p], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_w, ms_p = (float(v) for v in tt.tolist())
+    # ---- end to end: each step's inputs copied from pinned host memory ----
+    keys = ("model_vert", "model_norm", "model_rgba", "depth", "rgba")
+    host = [{k: getattr(p, k).cpu().pin_memory() for k in keys} for p in pool]
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(K):
+        for key in keys:
+            getattr(pool[k % 2], key).copy_(host[k % 2][key], non_blocking=True)
+        b.track_warm(net, fps[k % 2], descs=descs[k % 2], **wkw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([ms_e2e], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(tt.item())
+    # ---- roofline: the batched association kernel at level 0 ----
+    b.track(fps[0], descs=descs[0])
+    k_ms, s_ms, it_ms = b.time_iteration(0, reps=10)
+    px = nb * cam.width * cam.height
+    alg = PASS1_BYTES_PER_PX * px
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (k_ms * 1e-3) / 1e9
+    # ---- accuracy and iteration counts ----
+    def errs(res_list):
+        e = []
+        for k, res in enumerate(res_list):
+            T2 = pool[k % 2].T2
+            e += [synth.pose_error(np.array(r.pose, np.float64).reshape(4, 4), T2[i]) for i, r in enumerate(res)]
+        return np.array(e)
+    ew, ep = errs(res_w), errs(res_p)
+    pct = lambda v: {"p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90))}
+    fail = lambda e: float(np.mean((e[:, 0] > np.radians(2.0)) | (e[:, 1] > 0.05)))
+    it_w = np.array([list(r.iterations) for res in res_w for r in res], np.float64)
+    it_p = np.array([list(r.iterations) for res in res_p for r in res], np.float64)
+    fbr = float(np.mean(np.concatenate(fb_all)))
+    # kernels per warm step: packing + 8 GEMMs per 256 pairs, the warm graph
+    # (stamp, model maps, 2 photometric inputs, 4 pyramid steps, 2 depth
+    # pyramid steps, maps, derivatives, begin, seed, 2 per iteration, end) and
+    # the fall-back batch with its SO3 stage
+    gemm = -(-nb // 256) * 9
+    warm_graph = 13 + 2 * sum(its[:args.warm_levels])
+    plain_graph = 14 + 1 + 2 * 19
+    launches = K * (gemm + warm_graph + (plain_graph if fbr > 0 else 0))
+    return {"fps": K * nb / (ms_w * 1e-3), "ms_per_step": ms_w / K, "steps": K, "warmup": W, "batch_pairs": nb,
+            "pool_batches": 2, "batch_bytes": batch_bytes,
+            "schedule": {"levels": args.warm_levels, "iterations": list(its), "so3": False},
+            "fallback_cfg": {"residual_limit": wkw["residual_limit"], "residual_ratio": args.residual_ratio,
+                             "plain_residual_median": plain_res, "max_disagree_deg": args.max_disagree},
+            "train": {"pairs_rendered": args.train_pairs, "pairs_kept": n_train, "epochs": args.epochs,
+                      "generation_s": gen_s, "train_s": train_s, "last_epoch_loss": hist[-1]},
+            "launch": {"threads": threads, "pixels_per_thread": ppt},
+            "e2e": {"value": K * nb / (ms_e2e * 1e-3), "unit": "frames/s", "h2d_bytes_per_step": int(batch_bytes),
+                    "d2h_bytes_per_step": int(nb * ctypes_sizeof_result())},
+            "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres_b (level 0, all pairs of a step)",
+                         "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel_ms": k_ms, "photometric_kernel_ms": s_ms,
+                         "iteration_ms": it_ms, "alg_bytes_per_launch": alg,
+                         "alg_bytes_per_px": PASS1_BYTES_PER_PX},
+            "plain_batched": {"frames_per_s": K * nb / (ms_p * 1e-3), "ms_per_step": ms_p / K,
+                              "schedule": "SO3 + 10/5/4, the reference's"},
+            "pose_error_vs_gt": {"warm": {"rot_rad": pct(ew[:, 0]), "trans_m": pct(ew[:, 1]), "fail": fail(ew)},
+                                 "plain_batched": {"rot_rad": pct(ep[:, 0]), "trans_m": pct(ep[:, 1]),
+                                                   "fail": fail(ep)},
+                                 "fail_definition": "error > 2 deg or > 5 cm"},
+            "fallback_rate": fbr,
+            "iterations_mean": {"warm": it_w.mean(axis=0).tolist(), "plain_batched": it_p.mean(axis=0).tolist(),
+                                "order": ["so3", "L0", "L1", "L2"]},
+            "clocks": clk, "gpu_launches": int(launches)}
+
+
+def ctypes_sizeof_result():
+    import ctypes
+    from slam_gb300 import _native
+    return ctypes.sizeof(_native.OdoPairResult)
 
 
 def make_batch_pairs(n, seed, sizes="mixed"):
@@ -771,6 +949,9 @@ def run_warm_study(args):
 
 def main():
     args = parse()
+    if args.no_prefetch:
+        from slam_gb300 import _native
+        _native.load().odo_debug_set_prefetch(0)
     if args.study == "warm":
         run_warm_study(args)
         return

@@ -195,6 +195,11 @@ int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rg
                        int so3, odo_pair_result *scratch_results, int *threads, int *pixels_per_thread,
                        float *best_ms);
 const char *odo_batch_last_error(odo_batch_t *b);
+/* Times `reps` Gauss-Newton iterations at `level` over all pairs of the last
+ * odo_batch_track call (CUDA events on the batch stream): out_ms[0] / [1] the
+ * association and photometric/solve kernels alone, out_ms[2] both; restores
+ * the tracking states afterwards. */
+int odo_batch_debug_time_iteration(odo_batch_t *b, int level, int reps, float out_ms[3]);
 
 /* ---- parity / debugging access (used by the tests) ----
  * Buffer ids: 0 depth pyramid (u16), 1 vmap_curr, 2 nmap_curr, 3 vmap_prev,
@@ -248,6 +253,11 @@ int odo_debug_derivatives(odo_t *h);
  * photometric/solve kernel, each timed alone; out_ms[2] = mean time of one
  * whole iteration.  Leaves the tracking state as it found it. */
 int odo_debug_time_iteration(odo_t *h, int level, int reps, float out_ms[3]);
+
+/* Process-wide switch of the L2 bulk prefetch of the next pixel chunk in the
+ * iteration kernels (default 1); takes effect for calls made afterwards (a
+ * handle's or batch's captured graphs keep the value they were built with). */
+int odo_debug_set_prefetch(int on);
 
 /* Device-side phase timers accumulated over tracking calls (ns):
  * out[0] last-block reduction of the block partials, out[1] FP64 solve and

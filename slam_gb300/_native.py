@@ -112,6 +112,7 @@ SIGNATURES = [
     ("odo_debug_so3_step", c_int, [c_void_p, P(c_float), P(c_float), P(c_float), P(c_double)]),
     ("odo_debug_derivatives", c_int, [c_void_p]),
     ("odo_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
+    ("odo_debug_set_prefetch", c_int, [c_int]),
     ("odo_debug_profile", c_int, [c_void_p, P(c_double), c_int]),
     ("odo_debug_history", c_int, [c_void_p, P(c_double), c_int]),
     ("odo_cnn_param_count", c_size_t, []),
@@ -141,6 +142,7 @@ SIGNATURES = [
     ("odo_batch_set_stream", c_int, [c_void_p, c_void_p]),
     ("odo_batch_set_launch", c_int, [c_void_p, c_int, c_int]),
     ("odo_batch_track", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult)]),
+    ("odo_batch_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
     ("odo_batch_track_init", c_int, [c_void_p, P(OdoPair), c_int, c_void_p, c_int, c_float, c_int, P(OdoPairResult)]),
     ("odo_batch_autotune", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult),
                                    P(c_int), P(c_int), P(c_float)]),

@@ -130,6 +130,13 @@ class BatchOdometry:
                     "odo_batch_track_warm")
         return res, np.array(fb[:], bool)
 
+    def time_iteration(self, level, reps=20):
+        """Mean CUDA-event times (ms) over all pairs of the last track() call:
+        association kernel, photometric/solve kernel, one whole iteration."""
+        out = (ctypes.c_float * 3)()
+        self._check(self._L.odo_batch_debug_time_iteration(self._h, int(level), int(reps), out), "time_iteration")
+        return list(out)
+
     def autotune(self, pairs, rgbOnly=False, icpWeight=10.0, fastOdom=False, so3=True):
         descs = self._descs(pairs)
         res = (_native.OdoPairResult * len(pairs))()

@@ -69,6 +69,7 @@ struct odo_batch {
     int max_nb[kLevels];
     int max_w = 0, max_h = 0;
     float *init_dev = nullptr;  // [max_pairs][6] warm-start motions (odo_batch_track_init)
+    int last_n = 0, last_rgb = 0;  // pair count and photometric flag of the last tracking call
     std::map<GKey, cudaGraphExec_t> graphs;
     std::string last_error;
 };
@@ -344,6 +345,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             L.minScale = d.minScale[l];
             L.maxDepthDelta = 0.07f;
             L.sobelScale = sobelScale;
+            L.prefetch = g_l2_prefetch;  // the batch arena's own buffers
             a.st = b->st_dev + i;
             a.ws = p.ws;
             a.iters = (l < q.levels) ? (q.iterations[l] > 0 ? q.iterations[l] : base[l]) : 0;
@@ -558,6 +560,8 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
         BCK(cudaGraphLaunch(it->second, b->stream));
     }
     BCK(cudaStreamSynchronize(b->stream));
+    b->last_n = npairs;
+    b->last_rgb = rgb;
     for (int i = 0; i < npairs; ++i) {
         const TrackState &st = b->st_host[i];
         if (st.status != 0) return st.status;
@@ -648,6 +652,41 @@ int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, 
                     false);
     if (rc != ODO_OK) return rc;
     for (size_t k = 0; k < idx.size(); ++k) results[idx[k]] = sres[k];
+    return ODO_OK;
+}
+
+int odo_batch_debug_time_iteration(odo_batch_t *b, int level, int reps, float out_ms[3]) {
+    if (!b || level < 0 || level >= kLevels || reps < 1 || !out_ms || b->last_n < 1) return ODO_ERR_ARG;
+    const int n = b->last_n;
+    const PassArgs *args = (const PassArgs *)(b->args_dev + b->o_pass[level]);
+    cudaStream_t s = b->stream;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    cudaError_t e = cudaSuccess;
+    float ms[3] = {0, 0, 0};
+    for (int part = 0; part < 3 && e == cudaSuccess; ++part) {
+        const int mask = part == 2 ? 3 : part + 1;
+        // restore the states of the last call so every repetition does the same work
+        e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = launch_level_iteration_batch(args, n, b->max_nb[level], b->last_rgb ? b->max_nb[level] : 1, b->threads,
+                                             0, 1, s, 3);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+        for (int r = 0; r < reps && e == cudaSuccess; ++r)
+            e = launch_level_iteration_batch(args, n, b->max_nb[level], b->last_rgb ? b->max_nb[level] : 1, b->threads,
+                                             0, 1, s, mask);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[part], e0, e1);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return bfail(b, e, "odo_batch_debug_time_iteration");
+    for (int k = 0; k < 3; ++k) out_ms[k] = ms[k] / reps;
     return ODO_OK;
 }
 

@@ -40,17 +40,23 @@ __device__ __forceinline__ uint4 pack8(const uint16_t (&v)[8]) {
 __device__ __forceinline__ uint4 zero4() { return make_uint4(0, 0, 0, 0); }
 
 // ---------------------------------------------------------------- loaders
+// (interface: umma_gemm.cuh -- Row once per CTA row, Col once per K group)
+constexpr uint16_t kBf16One = 0x3F80;
+
 // Row-major BF16 [rows][ld], K columns used (ld % 8 == 0, 16-byte aligned base).
 struct LdDense {
     const uint16_t *p;
     int rows, K, ld;
-    __device__ uint4 operator()(int r, int k8) const {
-        const int k = k8 * 8;
-        if (r >= rows || k >= K) return zero4();
-        if (k + 8 <= K) return __ldg(reinterpret_cast<const uint4 *>(p + (size_t)r * ld + k));
+    using Row = const uint16_t *;
+    using Col = int;
+    __device__ Row row(int r) const { return r < rows ? p + (size_t)r * ld : nullptr; }
+    __device__ Col col(int k8) const { return k8 * 8; }
+    __device__ uint4 load(Row q, int k) const {
+        if (!q || k >= K) return zero4();
+        if (k + 8 <= K) return __ldg(reinterpret_cast<const uint4 *>(q + k));
         uint16_t v[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = (k + j < K) ? p[(size_t)r * ld + k + j] : 0;
+        for (int j = 0; j < 8; ++j) v[j] = (k + j < K) ? q[k + j] : 0;
         return pack8(v);
     }
 };
@@ -58,58 +64,71 @@ struct LdDense {
 struct LdDenseF32 {
     const float *p;
     int rows, K, ld;
-    __device__ uint4 operator()(int r, int k8) const {
+    using Row = const float *;
+    using Col = int;
+    __device__ Row row(int r) const { return r < rows ? p + (size_t)r * ld : nullptr; }
+    __device__ Col col(int k8) const { return k8 * 8; }
+    __device__ uint4 load(Row q, int k) const {
+        uint16_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = (q && k + j < K) ? f2bf(q[k + j]) : 0;
+        return pack8(v);
+    }
+};
+// Transposed view of a row-major matrix G[K][ld]: A(r, k) = G[k][r] (BF16,
+// or FP32 rounded to BF16).  ones_row >= 0: that row reads 1 for every
+// k < K (a bias column of a weight-gradient product).
+template <typename T>
+struct LdTransT {
+    const T *p;
+    int rows, K, ld, ones_row;
+    using Row = int;
+    using Col = int;
+    __device__ Row row(int r) const { return r == ones_row ? -2 : (r < rows ? r : -1); }
+    __device__ Col col(int k8) const { return k8 * 8; }
+    __device__ uint4 load(int r, int k0) const {
         uint16_t v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int k = k8 * 8 + j;
-            v[j] = (r < rows && k < K) ? f2bf(p[(size_t)r * ld + k]) : 0;
+            const int k = k0 + j;
+            uint16_t u = 0;
+            if (k < K) {
+                if (r == -2) u = kBf16One;
+                else if (r >= 0) {
+                    if constexpr (sizeof(T) == 4) u = f2bf(p[(size_t)k * ld + r]);
+                    else u = p[(size_t)k * ld + r];
+                }
+            }
+            v[j] = u;
         }
         return pack8(v);
     }
 };
-// Transposed view of a row-major BF16 matrix G[K][ld]: A(r, k) = G[k][r].
-struct LdTrans {
-    const uint16_t *p;
-    int rows, K, ld;
-    __device__ uint4 operator()(int r, int k8) const {
-        uint16_t v[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int k = k8 * 8 + j;
-            v[j] = (r < rows && k < K) ? p[(size_t)k * ld + r] : 0;
-        }
-        return pack8(v);
-    }
-};
-struct LdTransF32 {
-    const float *p;
-    int rows, K, ld;
-    __device__ uint4 operator()(int r, int k8) const {
-        uint16_t v[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int k = k8 * 8 + j;
-            v[j] = (r < rows && k < K) ? f2bf(p[(size_t)k * ld + r]) : 0;
-        }
-        return pack8(v);
-    }
-};
+using LdTrans = LdTransT<uint16_t>;
+using LdTransF32 = LdTransT<float>;
 
 // Geometry of one 3x3 / stride 2 / pad 1 convolution over NHWC input.
 struct ConvGeo {
     int B, H, W, C, Ho, Wo;
     __device__ int M() const { return B * Ho * Wo; }
-    // input element index of im2col(m, k), or -1 for padding
-    __device__ long long src(int m, int k) const {
-        const int tap = k / C, ci = k - tap * C;
-        const int ky = tap / 3, kx = tap - 3 * ky;
-        const int ox = m % Wo;
-        const int t = m / Wo;
-        const int oy = t % Ho, b = t / Ho;
-        const int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;
+    // output position m -> {pixel index of image b's origin, 2 oy - 1, 2 ox - 1, valid}
+    __device__ int4 pos(int m) const {
+        if (m >= M()) return make_int4(0, 0, 0, 0);
+        const int ox = m % Wo, t = m / Wo, oy = t % Ho, b = t / Ho;
+        return make_int4(b * H * W, 2 * oy - 1, 2 * ox - 1, 1);
+    }
+    // im2col column k -> {ky, kx, ci, valid}
+    __device__ int4 tap(int k) const {
+        if (k >= 9 * C) return make_int4(0, 0, 0, 0);
+        const int t = k / C, ci = k - t * C, ky = t / 3;
+        return make_int4(ky, t - 3 * ky, ci, 1);
+    }
+    // input element of (position, tap), or -1 for the zero padding
+    __device__ long long src(const int4 &p, const int4 &t) const {
+        if (!p.w || !t.w) return -1;
+        const int iy = p.y + t.x, ix = p.z + t.y;
         if (iy < 0 || iy >= H || ix < 0 || ix >= W) return -1;
-        return (((long long)b * H + iy) * W + ix) * C + ci;
+        return ((long long)p.x + (long long)iy * W + ix) * C + t.z;
     }
 };
 // Implicit im2col A(m, k) of an NHWC input; C % 8 == 0 so the 8 values of a
@@ -120,10 +139,12 @@ template <bool F16>
 struct LdIm2col {
     const uint16_t *x;
     ConvGeo g;
-    __device__ uint4 operator()(int m, int k8) const {
-        const int k = k8 * 8;
-        if (m >= g.M() || k >= 9 * g.C) return zero4();
-        const long long o = g.src(m, k);
+    using Row = int4;
+    using Col = int4;
+    __device__ Row row(int m) const { return g.pos(m); }
+    __device__ Col col(int k8) const { return g.tap(k8 * 8); }
+    __device__ uint4 load(const int4 &p, const int4 &t) const {
+        const long long o = g.src(p, t);
         if (o < 0) return zero4();
         uint4 v = __ldg(reinterpret_cast<const uint4 *>(x + o));
         if (!F16) return v;
@@ -134,20 +155,34 @@ struct LdIm2col {
         return pack8(b);
     }
 };
-// Transposed im2col: B(k, m) = im2col(m, k) for 8 consecutive positions m.
+// Transposed im2col: B(k, m) = im2col(m, k) for 8 consecutive positions m;
+// row k = 9 C reads 1 for every valid position (the bias column).
 template <bool F16>
 struct LdIm2colT {
     const uint16_t *x;
     ConvGeo g;
-    __device__ uint4 operator()(int k, int m8) const {
+    struct Col {
+        int4 p[8];
+    };
+    using Row = int4;  // tap; w = 0 invalid, 1 tap, 2 the ones row
+    __device__ Row row(int k) const {
+        if (k == 9 * g.C) return make_int4(0, 0, 0, 2);
+        return g.tap(k);
+    }
+    __device__ Col col(int m8) const {
+        Col c;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) c.p[j] = g.pos(m8 * 8 + j);
+        return c;
+    }
+    __device__ uint4 load(const int4 &t, const Col &c) const {
         uint16_t v[8];
-        const int M = g.M();
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int m = m8 * 8 + j;
             uint16_t u = 0;
-            if (k < 9 * g.C && m < M) {
-                const long long o = g.src(m, k);
+            if (t.w == 2) u = c.p[j].w ? kBf16One : 0;
+            else {
+                const long long o = g.src(c.p[j], t);
                 if (o >= 0) u = F16 ? h2bf(x[o]) : x[o];
             }
             v[j] = u;
@@ -167,6 +202,20 @@ struct EpBiasAct {  // y = act(v + bias) as BF16
     const float *bias;
     int N, ld, relu;
     __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+        if (n0 + 8 <= N && (ld & 7) == 0) {  // one 16-byte store (bias 32-byte aligned)
+            const float4 b0 = *reinterpret_cast<const float4 *>(bias + n0);
+            const float4 b1 = *reinterpret_cast<const float4 *>(bias + n0 + 4);
+            const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            uint16_t o[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float f = v[j] + bb[j];
+                if (relu) f = fmaxf(f, 0.f);
+                o[j] = f2bf(f);
+            }
+            *reinterpret_cast<uint4 *>(y + (size_t)m * ld + n0) = pack8(o);
+            return;
+        }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int n = n0 + j;
@@ -192,18 +241,32 @@ struct EpStore {
     float *y;
     int N, ld;
     __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+        if (n0 + 8 <= N && (ld & 3) == 0) {
+            float4 *q = reinterpret_cast<float4 *>(y + (size_t)m * ld + n0);
+            q[0] = make_float4(v[0], v[1], v[2], v[3]);
+            q[1] = make_float4(v[4], v[5], v[6], v[7]);
+            return;
+        }
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (n0 + j < N) y[(size_t)m * ld + n0 + j] = v[j];
     }
 };
-struct EpAtomic {
-    float *y;
-    int N, ld;
+// Weight gradient [rows][K] and, from column K, the bias gradient [rows];
+// atomic when the product is split over K.
+template <bool ATOMIC>
+struct EpWeightBias {
+    float *w, *bias;
+    int K;
     __device__ void operator()(int m, int n0, const float (&v)[8]) const {
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (n0 + j < N) atomicAdd(&y[(size_t)m * ld + n0 + j], v[j]);
+        for (int j = 0; j < 8; ++j) {
+            const int n = n0 + j;
+            float *dst = n < K ? w + (size_t)m * K + n : (n == K && bias ? bias + m : nullptr);
+            if (!dst) continue;
+            if (ATOMIC) atomicAdd(dst, v[j]);
+            else *dst = v[j];
+        }
     }
 };
 struct EpMask {  // dst = BF16(v) where the activation is positive, else 0
@@ -211,6 +274,16 @@ struct EpMask {  // dst = BF16(v) where the activation is positive, else 0
     const uint16_t *act;
     int N, ld;
     __device__ void operator()(int m, int n0, const float (&v)[8]) const {
+        if (n0 + 8 <= N && (ld & 7) == 0) {
+            const size_t o = (size_t)m * ld + n0;
+            const uint4 a4 = *reinterpret_cast<const uint4 *>(act + o);
+            const uint16_t *a = reinterpret_cast<const uint16_t *>(&a4);
+            uint16_t r[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) r[j] = bf2f(a[j]) > 0.f ? f2bf(v[j]) : (uint16_t)0;
+            *reinterpret_cast<uint4 *>(dst + o) = pack8(r);
+            return;
+        }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int n = n0 + j;
@@ -248,27 +321,6 @@ __global__ void k_col2im_mask(const float *dcol, const uint16_t *act, uint16_t *
             }
         }
         dpre[i] = bf2f(act[i]) > 0.f ? f2bf(s) : (uint16_t)0;
-    }
-}
-
-// db[n] += sum over rows m of g[m][n] (BF16 or FP32 rows of length ld)
-template <typename T>
-__global__ void k_colsum(const T *g, int M, int N, int ld, float *db) {
-    __shared__ float sm[8][33];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int n = blockIdx.x * 32 + tx;
-    float s = 0.f;
-    if (n < N)
-        for (int m = blockIdx.y * 8 + ty; m < M; m += gridDim.y * 8) {
-            if constexpr (sizeof(T) == 2) s += bf2f(g[(size_t)m * ld + n]);  // BF16 bits
-            else s += g[(size_t)m * ld + n];
-        }
-    sm[ty][tx] = s;
-    __syncthreads();
-    if (ty == 0 && n < N) {
-        float t = 0.f;
-        for (int k = 0; k < 8; ++k) t += sm[k][tx];
-        atomicAdd(&db[n], t);
     }
 }
 
@@ -435,16 +487,15 @@ cudaError_t cnn_backward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
     const ParamLayout &P = n.L;
     CNN_CK(cudaMemsetAsync(n.grad, 0, P.total * sizeof(float), s));
     const int l1 = kConv, l2 = kConv + 1;
-    // fc2
-    CNN_CK(gemm(LdTransF32{n.dout, kOut, B, kOut}, LdTrans{n.hid, kHidden, B, kHidden},
-                EpStore{n.grad + P.w[l2], kHidden, kHidden}, kOut, kHidden, B, 1, n.err, s));
-    k_colsum<float><<<dim3(1, 8), 256, 0, s>>>(n.dout, B, kOut, kOut, n.grad + P.b[l2]);
+    // fc2: weight gradient and, from the ones row of B, the bias gradient
+    CNN_CK(gemm(LdTransF32{n.dout, kOut, B, kOut, -1}, LdTrans{n.hid, kHidden, B, kHidden, kHidden},
+                EpWeightBias<false>{n.grad + P.w[l2], n.grad + P.b[l2], kHidden}, kOut, kHidden + 1, B, 1, n.err,
+                s));
     CNN_CK(gemm(LdDenseF32{n.dout, B, kOut, kOut}, LdDense{n.wt + P.wt[l2], kHidden, kOut, P.wt_ld[l2]},
                 EpMask{n.dpre_hid, n.hid, kHidden, kHidden}, B, kHidden, kOut, 1, n.err, s));
     // fc1
-    CNN_CK(gemm(LdTrans{n.dpre_hid, kHidden, B, kHidden}, LdTrans{n.act[kConv], kFlat, B, kFlat},
-                EpStore{n.grad + P.w[l1], kFlat, kFlat}, kHidden, kFlat, B, 1, n.err, s));
-    k_colsum<uint16_t><<<dim3((kHidden + 31) / 32, 8), 256, 0, s>>>(n.dpre_hid, B, kHidden, kHidden, n.grad + P.b[l1]);
+    CNN_CK(gemm(LdTrans{n.dpre_hid, kHidden, B, kHidden, -1}, LdTrans{n.act[kConv], kFlat, B, kFlat, kFlat},
+                EpWeightBias<false>{n.grad + P.w[l1], n.grad + P.b[l1], kFlat}, kHidden, kFlat + 1, B, 1, n.err, s));
     CNN_CK(gemm(LdDense{n.dpre_hid, B, kHidden, kHidden}, LdDense{n.wt + P.wt[l1], kFlat, kHidden, P.wt_ld[l1]},
                 EpMask{n.dpre[kConv], n.act[kConv], kFlat, kFlat}, B, kFlat, kHidden, 1, n.err, s));
     CNN_CK(cudaGetLastError());
@@ -453,18 +504,19 @@ cudaError_t cnn_backward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
         const ConvGeo g = conv_geo(l, B);
         const int Mpos = B * g.Ho * g.Wo, Co = kCout[l], K = 9 * kCin[l];
         const uint16_t *dp = n.dpre[l + 1];
-        // weight gradient, split over positions
+        // weight gradient (columns 0..K-1) and bias gradient (column K, the
+        // ones row of the transposed im2col), split over positions
         const int kchunks = (Mpos + kGemmKChunk - 1) / kGemmKChunk;
-        const int tiles = (K + 127) / 128;
+        const int tiles = (K + 1 + 127) / 128;
         int splits = 2 * 152 / tiles;
         if (splits > kchunks) splits = kchunks;
         if (splits < 1) splits = 1;
-        const LdTrans da{dp, Co, Mpos, Co};
-        const EpAtomic ew{n.grad + P.w[l], K, K};
-        if (l == 0) CNN_CK(launch_umma_gemm<128>(da, LdIm2colT<true>{input, g}, ew, Co, K, Mpos, splits, 0, n.err, s));
-        else CNN_CK(launch_umma_gemm<128>(da, LdIm2colT<false>{n.act[l], g}, ew, Co, K, Mpos, splits, 0, n.err, s));
-        k_colsum<uint16_t><<<dim3((Co + 31) / 32, 64), 256, 0, s>>>(dp, Mpos, Co, Co, n.grad + P.b[l]);
-        CNN_CK(cudaGetLastError());
+        const LdTrans da{dp, Co, Mpos, Co, -1};
+        const EpWeightBias<true> ew{n.grad + P.w[l], n.grad + P.b[l], K};
+        if (l == 0)
+            CNN_CK(launch_umma_gemm<128>(da, LdIm2colT<true>{input, g}, ew, Co, K + 1, Mpos, splits, 0, n.err, s));
+        else
+            CNN_CK(launch_umma_gemm<128>(da, LdIm2colT<false>{n.act[l], g}, ew, Co, K + 1, Mpos, splits, 0, n.err, s));
         if (l == 0) break;
         // data gradient
         CNN_CK(gemm(LdDense{dp, Mpos, Co, Co}, LdDense{n.wt + P.wt[l], K, Co, P.wt_ld[l]}, EpStore{n.dcol, K, K},

@@ -165,7 +165,8 @@ cudaError_t enqueue_derivatives(odo_t *h, cudaStream_t s) {
 }
 
 LevelArgs level_args(odo_t *h, int l) {
-    LevelArgs L;
+    LevelArgs L{};
+    L.prefetch = g_l2_prefetch;  // all of the handle's buffers are its own
     L.level = l;
     L.cols = h->dims_w[l];
     L.rows = h->dims_h[l];
@@ -672,6 +673,11 @@ int odo_debug_history(odo_t *h, double *out, int max_rows) {
     for (int r = 0; r < n; ++r)
         for (int k = 0; k < 9; ++k) out[r * 9 + k] = h->st_host->hist[r][k];
     return n;
+}
+
+int odo_debug_set_prefetch(int on) {
+    g_l2_prefetch = on ? 1 : 0;
+    return ODO_OK;
 }
 
 int odo_debug_profile(odo_t *h, double out[8], int reset) {

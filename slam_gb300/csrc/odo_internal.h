@@ -91,6 +91,7 @@ struct LevelArgs {
     Img<const uint8_t> lastImage, nextImage;
     Img<Corr> corr;
     Img<const uint8_t> cand;  // pose-independent photometric preconditions, per pixel
+    int prefetch;             // 1: every buffer above is the library's own (L2 bulk prefetch allowed)
     float minScale;
     float maxDepthDelta;
     float sobelScale;
@@ -225,8 +226,12 @@ cudaError_t launch_stamp_batch(TrackState *states, int npairs, cudaStream_t s);
 cudaError_t launch_warm_seed_batch(TrackState *states, const float *init, int npairs, cudaStream_t s);
 cudaError_t launch_track_end_batch(TrackState *states, int npairs, cudaStream_t s);
 cudaError_t launch_so3_batch(const So3Args *args, int npairs, cudaStream_t s);
+// parts: bit 0 the association/residual kernel, bit 1 the photometric/solve kernel
 cudaError_t launch_level_iteration_batch(const PassArgs *args, int npairs, int max_nb_icp, int max_nb_rgb,
-                                         int threads, int precision, int iter, cudaStream_t s);
+                                         int threads, int precision, int iter, cudaStream_t s, int parts = 3);
+
+// process-wide switch of the iteration kernels' L2 bulk prefetch (default on)
+extern int g_l2_prefetch;
 
 // debug single passes
 cudaError_t launch_debug_icp(const LevelArgs &L, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],

@@ -11,7 +11,12 @@
 // and hands 8 consecutive columns of a row at a time to the epilogue functor.
 // gridDim.z > 1 splits K (the epilogue then accumulates, e.g. atomically).
 //
-// Loader:   __device__ uint4 operator()(int row, int k8) const   (k = 8 k8 .. 8 k8 + 7)
+// Loader (index work split so that it is paid once per row and once per K
+// group, not per load):
+//   typename Row; __device__ Row row(int r) const;     once per CTA and row
+//   typename Col; __device__ Col col(int k8) const;    once per K chunk (k = 8 k8 .. 8 k8 + 7)
+//   __device__ uint4 load(const Row &, const Col &) const;   8 16-bit values
+// Every thread stages a fixed K group of 8 A rows (and BN / 16 B rows).
 // Epilogue: __device__ void operator()(int m, int n0, const float (&v)[8]) const
 #pragma once
 #include <cstdint>
@@ -62,6 +67,16 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
     umma::fence_after_sync();
     const uint32_t tmem = tmem_base;
     const uint32_t lbo = layout ? 1024u : 128u, sbo = layout ? 128u : 1024u;
+    // thread t writes the 16-byte slots t + 128 j: row group (t >> 6) + 2 j,
+    // K group (t >> 3) & 7, row (t & 7) -- conflict-free 16-byte stores
+    constexpr int AR = 8, BR = BN / 16;
+    const int kg = (tid >> 3) & 7;
+    typename LA::Row ra[AR];
+    typename LB::Row rb[BR];
+#pragma unroll
+    for (int j = 0; j < AR; ++j) ra[j] = la.row(m0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
+#pragma unroll
+    for (int j = 0; j < BR; ++j) rb[j] = lb.row(n0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
     bool ok = true;
     int c = 0;
     for (; c < nch; ++c) {
@@ -74,18 +89,16 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
             ok = umma::mbar_wait(&mbar[s], ((c - 2) >> 1) & 1, kGemmWaitPolls);
             if (!__syncthreads_and(ok)) break;
         }
-        const int k8_0 = (c_begin + c) * (kGemmKChunk / 8);
-        // thread i writes bytes [16 i, 16 i + 16): row group i >> 6, K group
-        // (i >> 3) & 7, row (i & 7) -- conflict-free 16-byte stores
-#pragma unroll 4
-        for (int i = tid; i < 128 * 8; i += kGemmThreads) {
-            const int row = ((i >> 6) << 3) + (i & 7), kg = (i >> 3) & 7;
-            *reinterpret_cast<uint4 *>(sa + i * 16) = la(m0 + row, k8_0 + kg);
+        const int k8 = (c_begin + c) * (kGemmKChunk / 8) + kg;
+        {
+            const typename LA::Col ca = la.col(k8);
+#pragma unroll
+            for (int j = 0; j < AR; ++j) *reinterpret_cast<uint4 *>(sa + (tid + 128 * j) * 16) = la.load(ra[j], ca);
         }
-#pragma unroll 4
-        for (int i = tid; i < BN * 8; i += kGemmThreads) {
-            const int row = ((i >> 6) << 3) + (i & 7), kg = (i >> 3) & 7;
-            *reinterpret_cast<uint4 *>(sb + i * 16) = lb(n0 + row, k8_0 + kg);
+        {
+            const typename LB::Col cb = lb.col(k8);
+#pragma unroll
+            for (int j = 0; j < BR; ++j) *reinterpret_cast<uint4 *>(sb + (tid + 128 * j) * 16) = lb.load(rb[j], cb);
         }
         umma::fence_smem_to_async();
         __syncthreads();

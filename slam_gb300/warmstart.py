@@ -253,6 +253,7 @@ def label_pairs(batch, pairset, chunk=512, agree_deg=1.0, agree_m=0.02):
     from .synth import pose_error
     labels = np.zeros((pairset.n, 6), np.float32)
     ok = np.zeros(pairset.n, bool)
+    chunk = min(chunk, batch.max_pairs)
     for s in range(0, pairset.n, chunk):
         idx = list(range(s, min(pairset.n, s + chunk)))
         res = track_plain(batch, pairset, idx)
@@ -371,6 +372,7 @@ def _label_with_residual(batch, pairset, chunk=512, agree_deg=0.5, agree_m=0.02)
     labels = np.zeros((pairset.n, 6), np.float32)
     ok = np.zeros(pairset.n, bool)
     err = np.zeros(pairset.n, np.float32)
+    chunk = min(chunk, batch.max_pairs)
     for s in range(0, pairset.n, chunk):
         idx = list(range(s, min(pairset.n, s + chunk)))
         res = track_plain(batch, pairset, idx)
