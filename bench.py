@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
-    ap.add_argument("--no-prefetch", action="store_true", help="disable the iteration kernels' L2 bulk prefetch")
+    ap.add_argument("--prefetch", action="store_true", help="enable the iteration kernels' L2 bulk prefetch")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
     ap.add_argument("--train-pairs", type=int, default=50000, help="warm study: rendered training pairs")
@@ -949,9 +949,9 @@ def run_warm_study(args):
 
 def main():
     args = parse()
-    if args.no_prefetch:
+    if args.prefetch:
         from slam_gb300 import _native
-        _native.load().odo_debug_set_prefetch(0)
+        _native.load().odo_debug_set_prefetch(1)
     if args.study == "warm":
         run_warm_study(args)
         return

@@ -5,8 +5,9 @@
  * The network has no counterpart in the reference; this file restates the
  * architecture and the training loss of the GPU implementation in plain C
  * with FP64 accumulation:
- *   input [B][120][160][8] FP16 NHWC, six 3x3 / stride 2 / pad 1 convolutions
- *   8->32->64->128->128->128->128 with ReLU, fc 768->768 ReLU, fc 768->6,
+ *   input [B][120][160][8] FP16 NHWC, six stride-2 convolutions with ReLU
+ *   (7x7 / pad 3: 8->32, then 3x3 / pad 1: ->64->128->128->128->128),
+ *   fc 768->768 ReLU, fc 768->6,
  *   loss = mean_b e^T M e, e = out - label, M a symmetric 6x6 metric.
  * rounding = 1 reproduces the GPU's rounding points (FP16 input and FP16
  * first-layer weights in the forward pass, BF16 weights, activations and
@@ -33,9 +34,10 @@ static const int CIN[NCONV] = {8, 32, 64, 128, 128, 128};
 static const int COUT[NCONV] = {32, 64, 128, 128, 128, 128};
 static const int HH[NCONV + 1] = {120, 60, 30, 15, 8, 4, 2};
 static const int WW[NCONV + 1] = {160, 80, 40, 20, 10, 5, 3};
+static const int KS[NCONV] = {7, 3, 3, 3, 3, 3};
 
 static int w_rows(int l) { return l < NCONV ? COUT[l] : (l == NCONV ? HIDDEN : NOUT); }
-static int w_cols(int l) { return l < NCONV ? 9 * CIN[l] : (l == NCONV ? FLAT : HIDDEN); }
+static int w_cols(int l) { return l < NCONV ? KS[l] * KS[l] * CIN[l] : (l == NCONV ? FLAT : HIDDEN); }
 
 /* parameter offsets: W then b per layer, each layer start rounded to 8 floats */
 void cnn_layout(size_t w[NLAYERS], size_t b[NLAYERS], size_t *total) {
@@ -87,9 +89,10 @@ static double half_to_double(uint16_t h) {
 static long conv_src(int l, int B, int m, int k) {
     const int C = CIN[l], H = HH[l], W = WW[l], Ho = HH[l + 1], Wo = WW[l + 1];
     (void)B;
-    const int tap = k / C, ci = k % C, ky = tap / 3, kx = tap % 3;
+    const int ks = KS[l], pad = (ks - 1) / 2;
+    const int tap = k / C, ci = k % C, ky = tap / ks, kx = tap % ks;
     const int ox = m % Wo, t = m / Wo, oy = t % Ho, b = t / Ho;
-    const int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;
+    const int iy = 2 * oy - pad + ky, ix = 2 * ox - pad + kx;
     if (iy < 0 || iy >= H || ix < 0 || ix >= W) return -1;
     return (((long)b * H + iy) * W + ix) * C + ci;
 }
@@ -111,10 +114,10 @@ int cnn_oracle_run(const double *params, const uint16_t *input, const double *la
         in16[i] = half_to_double(input[i]);
         act[0][i] = rb(in16[i]);
     }
-    for (size_t i = 0; i < (size_t)COUT[0] * 9 * CIN[0]; ++i) w[wo[0] + i] = rh(params[wo[0] + i]);
+    for (size_t i = 0; i < (size_t)COUT[0] * w_cols(0); ++i) w[wo[0] + i] = rh(params[wo[0] + i]);
     /* convolutions */
     for (int l = 0; l < NCONV; ++l) {
-        const int M = B * HH[l + 1] * WW[l + 1], N = COUT[l], K = 9 * CIN[l];
+        const int M = B * HH[l + 1] * WW[l + 1], N = COUT[l], K = w_cols(l);
         act[l + 1] = malloc((size_t)M * N * sizeof(double));
         double *y = act[l + 1];
         const double *x = l == 0 ? in16 : act[l];
@@ -205,7 +208,7 @@ int cnn_oracle_run(const double *params, const uint16_t *input, const double *la
         free(dh);
         /* convolutions, last to first; dpre = gradient at conv l's pre-activation */
         for (int l = NCONV - 1; l >= 0; --l) {
-            const int M = B * HH[l + 1] * WW[l + 1], Co = COUT[l], K = 9 * CIN[l];
+            const int M = B * HH[l + 1] * WW[l + 1], Co = COUT[l], K = w_cols(l);
             const double *x = act[l];
 #pragma omp parallel for schedule(static)
             for (int co = 0; co < Co; ++co) {

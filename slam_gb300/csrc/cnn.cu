@@ -107,21 +107,23 @@ struct LdTransT {
 using LdTrans = LdTransT<uint16_t>;
 using LdTransF32 = LdTransT<float>;
 
-// Geometry of one 3x3 / stride 2 / pad 1 convolution over NHWC input.
+// Geometry of one ks x ks / stride 2 / pad (ks - 1) / 2 convolution over NHWC input.
 struct ConvGeo {
-    int B, H, W, C, Ho, Wo;
+    int B, H, W, C, Ho, Wo, ks;
+    __device__ int pad() const { return (ks - 1) >> 1; }
+    __device__ int K() const { return ks * ks * C; }
     __device__ int M() const { return B * Ho * Wo; }
     // output position m -> {pixel index of image b's origin, 2 oy - 1, 2 ox - 1, valid}
     __device__ int4 pos(int m) const {
         if (m >= M()) return make_int4(0, 0, 0, 0);
         const int ox = m % Wo, t = m / Wo, oy = t % Ho, b = t / Ho;
-        return make_int4(b * H * W, 2 * oy - 1, 2 * ox - 1, 1);
+        return make_int4(b * H * W, 2 * oy - pad(), 2 * ox - pad(), 1);
     }
     // im2col column k -> {ky, kx, ci, valid}
     __device__ int4 tap(int k) const {
-        if (k >= 9 * C) return make_int4(0, 0, 0, 0);
-        const int t = k / C, ci = k - t * C, ky = t / 3;
-        return make_int4(ky, t - 3 * ky, ci, 1);
+        if (k >= K()) return make_int4(0, 0, 0, 0);
+        const int t = k / C, ci = k - t * C, ky = t / ks;
+        return make_int4(ky, t - ks * ky, ci, 1);
     }
     // input element of (position, tap), or -1 for the zero padding
     __device__ long long src(const int4 &p, const int4 &t) const {
@@ -156,7 +158,7 @@ struct LdIm2col {
     }
 };
 // Transposed im2col: B(k, m) = im2col(m, k) for 8 consecutive positions m;
-// row k = 9 C reads 1 for every valid position (the bias column).
+// row k = K reads 1 for every valid position (the bias column).
 template <bool F16>
 struct LdIm2colT {
     const uint16_t *x;
@@ -166,7 +168,7 @@ struct LdIm2colT {
     };
     using Row = int4;  // tap; w = 0 invalid, 1 tap, 2 the ones row
     __device__ Row row(int k) const {
-        if (k == 9 * g.C) return make_int4(0, 0, 0, 2);
+        if (k == g.K()) return make_int4(0, 0, 0, 2);
         return g.tap(k);
     }
     __device__ Col col(int m8) const {
@@ -296,6 +298,8 @@ struct EpMask {  // dst = BF16(v) where the activation is positive, else 0
 };
 
 // ---------------------------------------------------------------- kernels
+// Data gradient of a 3x3 / stride 2 / pad 1 layer (conv2..6; the first
+// layer needs none) gathered from dcol in the tap order (ky, kx).
 __global__ void k_col2im_mask(const float *dcol, const uint16_t *act, uint16_t *dpre, int B, int H, int W, int C,
                               int Ho, int Wo) {
     const long long n = (long long)B * H * W * C;
@@ -380,9 +384,10 @@ __global__ void k_transpose_bf16(const uint16_t *w, int rows, int cols, uint16_t
 // Network input of pair blockIdx.z: s x s block means of the valid depths
 // (metres; 0 where no pixel is valid) and of the intensities (the tracker's
 // weighting of the RGBA bytes, 0..1) of both frames, FP16; channels 4-7 are
-// derived from them in FP32 before rounding: live - model intensity, live -
-// model depth (0 unless both are valid), and the valid-depth fractions of the
-// two blocks (the differences keep the precision that FP16 depth loses).
+// derived from them in FP32 before rounding: 4 x (live - model intensity),
+// 10 x (live - model depth) (0 unless both are valid), and the valid-depth
+// fractions of the two blocks (the differences keep the precision that FP16
+// depth loses).
 __global__ void k_pack(const PackArgs *args, uint16_t *out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= kInW || y >= kInH) return;
@@ -422,8 +427,8 @@ __global__ void k_pack(const PackArgs *args, uint16_t *out) {
     h[1] = __float2half_rn(gm);
     h[2] = __float2half_rn(dl);
     h[3] = __float2half_rn(gl);
-    h[4] = __float2half_rn(gl - gm);
-    h[5] = __float2half_rn((nm && nl) ? dl - dm : 0.f);
+    h[4] = __float2half_rn(4.f * (gl - gm));                   // x4: differences are small
+    h[5] = __float2half_rn((nm && nl) ? 10.f * (dl - dm) : 0.f);  // decimetres
     h[6] = __float2half_rn(nm * invn);
     h[7] = __float2half_rn(nl * invn);
     uint16_t *o = out + (((size_t)blockIdx.z * kInH + y) * kInW + x) * kInC;
@@ -437,7 +442,7 @@ int grid_for(long long n, int threads) {
 }
 
 // Conv layer l geometry for batch B.
-ConvGeo conv_geo(int l, int B) { return ConvGeo{B, kH[l], kW[l], kCin[l], kH[l + 1], kW[l + 1]}; }
+ConvGeo conv_geo(int l, int B) { return ConvGeo{B, kH[l], kW[l], kCin[l], kH[l + 1], kW[l + 1], kKs[l]}; }
 
 template <bool F16 = false, class LA, class LB, class EP>
 cudaError_t gemm(const LA &a, const LB &b, const EP &e, int M, int N, int K, int splits, int *err, cudaStream_t s) {
@@ -458,7 +463,7 @@ cudaError_t cnn_forward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
     const ParamLayout &P = n.L;
     for (int l = 0; l < kConv; ++l) {
         const ConvGeo g = conv_geo(l, B);
-        const int M = B * g.Ho * g.Wo, N = kCout[l], K = 9 * kCin[l];
+        const int M = B * g.Ho * g.Wo, N = kCout[l], K = w_cols(l);
         const EpBiasAct ep{n.act[l + 1], n.master + P.b[l], N, N, 1};
         // the first layer in FP16 (the FP16 depth keeps 11 significant bits)
         if (l == 0) CNN_CK(gemm<true>(LdIm2col<false>{input, g}, LdDense{n.wh, N, K, K}, ep, M, N, K, 1, n.err, s));
@@ -502,7 +507,7 @@ cudaError_t cnn_backward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
     // conv layers, last to first
     for (int l = kConv - 1; l >= 0; --l) {
         const ConvGeo g = conv_geo(l, B);
-        const int Mpos = B * g.Ho * g.Wo, Co = kCout[l], K = 9 * kCin[l];
+        const int Mpos = B * g.Ho * g.Wo, Co = kCout[l], K = w_cols(l);
         const uint16_t *dp = n.dpre[l + 1];
         // weight gradient (columns 0..K-1) and bias gradient (column K, the
         // ones row of the transposed im2col), split over positions

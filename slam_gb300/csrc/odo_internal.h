@@ -230,7 +230,7 @@ cudaError_t launch_so3_batch(const So3Args *args, int npairs, cudaStream_t s);
 cudaError_t launch_level_iteration_batch(const PassArgs *args, int npairs, int max_nb_icp, int max_nb_rgb,
                                          int threads, int precision, int iter, cudaStream_t s, int parts = 3);
 
-// process-wide switch of the iteration kernels' L2 bulk prefetch (default on)
+// process-wide switch of the iteration kernels' L2 bulk prefetch (default off)
 extern int g_l2_prefetch;
 
 // debug single passes

@@ -14,10 +14,10 @@ def orc(built):
 def _params(orc, rng):
     w, b, total = orc.cnn_layout()
     rows = [32, 64, 128, 128, 128, 128, 768, 6]
-    cols = [72, 288, 576, 1152, 1152, 1152, 768, 768]
+    cols = [392, 288, 576, 1152, 1152, 1152, 768, 768]
     p = np.zeros(total)
     for l in range(8):
-        fan = 36 if l == 0 else cols[l]
+        fan = cols[l]
         sd = np.sqrt(2.0 / fan) if l < 7 else 0.1 * np.sqrt(1.0 / fan)
         p[w[l]:w[l] + rows[l] * cols[l]] = rng.normal(0, sd, rows[l] * cols[l])
         p[b[l]:b[l] + rows[l]] = rng.normal(0, 0.01, rows[l])
