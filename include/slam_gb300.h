@@ -309,12 +309,12 @@ int odo_icp_step_noalloc(const float *vmap_curr, const float *nmap_curr, const f
  * frames' 160x120 depth and gray images; forward and backward products run
  * on the tcgen05 tensor cores (FP32 accumulation).
  * Input [B][120][160][8] FP16 NHWC: model depth (m), model gray (0..1), live
- * depth (m), live gray, and four channels derived from them: 4 x (live -
- * model gray), 10 x (live - model depth), valid-depth fractions of the model
- * and live blocks.  Output [B][6]: translation (m)
+ * depth (m), live gray, and four channels derived from them: 2 x (live -
+ * model gray), 4 x (live - model depth, clamped to +-0.25 m), valid-depth
+ * fractions of the model and live blocks.  Output [B][6]: translation (m)
  * and rotation vector (rad) of the live camera in the model camera's frame.
- * Six stride-2 convolutions (7x7 8->32, then 3x3 ->64->128->128->128->128,
- * ReLU; the first one with FP16 operands, the others BF16), fc
+ * Six 3x3/stride-2 convolutions (8->32->64->128->128->128->128, ReLU; the
+ * first one with FP16 operands, the others BF16), fc
  * 768->768 (ReLU), fc 768->6; odo_cnn_param_count() FP32 parameters.
  * Loss: mean over the batch of e^T M e, e = out - label, M a symmetric 6x6
  * metric (default diag(100, 100, 100, 36, 36, 36)); Adam. */

@@ -5,8 +5,8 @@
  * The network has no counterpart in the reference; this file restates the
  * architecture and the training loss of the GPU implementation in plain C
  * with FP64 accumulation:
- *   input [B][120][160][8] FP16 NHWC, six stride-2 convolutions with ReLU
- *   (7x7 / pad 3: 8->32, then 3x3 / pad 1: ->64->128->128->128->128),
+ *   input [B][120][160][8] FP16 NHWC, six 3x3 / stride 2 / pad 1 convolutions
+ *   8->32->64->128->128->128->128 with ReLU,
  *   fc 768->768 ReLU, fc 768->6,
  *   loss = mean_b e^T M e, e = out - label, M a symmetric 6x6 metric.
  * rounding = 1 reproduces the GPU's rounding points (FP16 input and FP16
@@ -34,7 +34,7 @@ static const int CIN[NCONV] = {8, 32, 64, 128, 128, 128};
 static const int COUT[NCONV] = {32, 64, 128, 128, 128, 128};
 static const int HH[NCONV + 1] = {120, 60, 30, 15, 8, 4, 2};
 static const int WW[NCONV + 1] = {160, 80, 40, 20, 10, 5, 3};
-static const int KS[NCONV] = {7, 3, 3, 3, 3, 3};
+static const int KS[NCONV] = {3, 3, 3, 3, 3, 3};
 
 static int w_rows(int l) { return l < NCONV ? COUT[l] : (l == NCONV ? HIDDEN : NOUT); }
 static int w_cols(int l) { return l < NCONV ? KS[l] * KS[l] * CIN[l] : (l == NCONV ? FLAT : HIDDEN); }

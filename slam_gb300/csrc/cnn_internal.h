@@ -3,9 +3,9 @@
 //
 // Input  [B, 120, 160, 8] FP16 NHWC: model depth (m), model gray (0..1),
 //        live depth (m), live gray, four zero channels (16-byte rows).
-// conv1     7x7, stride 2, pad 3, ReLU: 8->32 (a wide first window: the
-//           frames are compared before any resolution is lost)
-// conv2..6  3x3, stride 2, pad 1, ReLU: 32->64->128->128->128->128
+// conv1..6  3x3, stride 2, pad 1, ReLU: 8->32->64->128->128->128->128
+//           (a 7x7 first layer was tried: with Adam's scale-free steps its
+//           392-wide fan-in over metre-valued depth made training unstable)
 //           (120x160 -> 60x80 -> 30x40 -> 15x20 -> 8x10 -> 4x5 -> 2x3)
 // fc1       768 -> 768, ReLU;  fc2  768 -> 6 (translation m, rotation vector rad)
 // Weights are stored [out][in] with the conv input index (ky * 3 + kx) * Cin + ci;
@@ -23,7 +23,7 @@ constexpr int kInH = 120, kInW = 160, kInC = 8;
 constexpr int kConv = 6;
 constexpr int kCin[kConv] = {8, 32, 64, 128, 128, 128};
 constexpr int kCout[kConv] = {32, 64, 128, 128, 128, 128};
-constexpr int kKs[kConv] = {7, 3, 3, 3, 3, 3};  // square kernel size (pad (k - 1) / 2, stride 2)
+constexpr int kKs[kConv] = {3, 3, 3, 3, 3, 3};  // square kernel size (pad (k - 1) / 2, stride 2)
 constexpr int kH[kConv + 1] = {120, 60, 30, 15, 8, 4, 2};
 constexpr int kW[kConv + 1] = {160, 80, 40, 20, 10, 5, 3};
 constexpr int kFlat = 2 * 3 * 128;

@@ -14,7 +14,7 @@ def orc(built):
 def _params(orc, rng):
     w, b, total = orc.cnn_layout()
     rows = [32, 64, 128, 128, 128, 128, 768, 6]
-    cols = [392, 288, 576, 1152, 1152, 1152, 768, 768]
+    cols = [72, 288, 576, 1152, 1152, 1152, 768, 768]
     p = np.zeros(total)
     for l in range(8):
         fan = cols[l]

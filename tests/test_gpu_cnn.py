@@ -120,7 +120,7 @@ def test_cnn_gradients_match_oracle(gpu, orc):
     assert abs(loss - loss_ref) <= 1e-2 * abs(loss_ref)
     w, b, total = orc.cnn_layout()
     rows = [32, 64, 128, 128, 128, 128, 768, 6]
-    cols = [392, 288, 576, 1152, 1152, 1152, 768, 768]
+    cols = [72, 288, 576, 1152, 1152, 1152, 768, 768]
     for l in range(8):
         for name, off, n in (("W", w[l], rows[l] * cols[l]), ("b", b[l], rows[l])):
             a, r = g[off:off + n].astype(np.float64), g_ref[off:off + n]

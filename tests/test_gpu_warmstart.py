@@ -19,7 +19,7 @@ def trained(gpu):
     net.set_loss_metric(ts["metric"])
     x0, y0 = ts["inputs"][:256].contiguous(), ts["labels"][:256].contiguous()
     loss0 = net.gradients(x0, y0)[1]
-    ws.train(net, ts["inputs"], ts["labels"], epochs=8, batch=256, lr=1e-3, lr_final=3e-5)
+    ws.train(net, ts["inputs"], ts["labels"], epochs=24, batch=256, lr=5e-4, lr_final=2e-5)
     loss1 = net.gradients(x0, y0)[1]
     ps = ws.make_room_pairs(4242, 256, synth.Camera(), 10.0, 0.10)
     return b, net, ps, float(np.median(ts["residuals"])), (loss0, loss1)
