@@ -68,8 +68,11 @@ int odo_create(int width, int height, float cx, float cy, float fx, float fy, fl
                odo_t **out);
 int odo_destroy(odo_t *h);
 
-/* Use `stream` (a cudaStream_t) for all work of this handle; NULL restores
- * the handle's own stream. */
+/* Use `stream` (a cudaStream_t) for all work of this handle.  NULL (the
+ * default) means the legacy default stream: the handle then works on its own
+ * stream (its CUDA graphs cannot be captured on the legacy stream) and orders
+ * every call after the work already queued on the legacy default stream,
+ * where the caller produced its inputs. */
 int odo_set_stream(odo_t *h, void *stream);
 
 /* initICP(GPUTexture* filteredDepth, depthCutoff), src/odom/RGBDOdometryef.cpp:118-142 */
@@ -176,6 +179,7 @@ typedef struct {
 
 int odo_batch_create(int max_pairs, odo_batch_t **out);
 int odo_batch_destroy(odo_batch_t *b);
+/* stream: as odo_set_stream (NULL: follow the legacy default stream). */
 int odo_batch_set_stream(odo_batch_t *b, void *stream);
 /* Launch shape of the two iteration kernels: threads per block (128 or 256)
  * and pixels per thread (each pair gets ceil(pixels / (threads * ppt))
@@ -309,9 +313,9 @@ int odo_icp_step_noalloc(const float *vmap_curr, const float *nmap_curr, const f
  * frames' 160x120 depth and gray images; forward and backward products run
  * on the tcgen05 tensor cores (FP32 accumulation).
  * Input [B][120][160][8] FP16 NHWC: model depth (m), model gray (0..1), live
- * depth (m), live gray, and four channels derived from them: 2 x (live -
- * model gray), 4 x (live - model depth, clamped to +-0.25 m), valid-depth
- * fractions of the model and live blocks.  Output [B][6]: translation (m)
+ * depth (m), live gray, and four channels derived from them: live - model
+ * gray, live - model depth, valid-depth fractions of the model and live
+ * blocks.  Output [B][6]: translation (m)
  * and rotation vector (rad) of the live camera in the model camera's frame.
  * Six 3x3/stride-2 convolutions (8->32->64->128->128->128->128, ReLU; the
  * first one with FP16 operands, the others BF16), fc
@@ -322,6 +326,7 @@ typedef struct odo_cnn odo_cnn_t;
 size_t odo_cnn_param_count(void);
 int odo_cnn_create(int max_batch, odo_cnn_t **out);
 int odo_cnn_destroy(odo_cnn_t *n);
+/* stream: all work of the network; NULL = the legacy default stream itself. */
 int odo_cnn_set_stream(odo_cnn_t *n, void *stream);
 int odo_cnn_init_params(odo_cnn_t *n, uint64_t seed);          /* He-normal weights, zero biases */
 int odo_cnn_set_params(odo_cnn_t *n, const float *host_params); /* also resets the optimiser */

@@ -70,6 +70,8 @@ struct odo_batch {
     int max_w = 0, max_h = 0;
     float *init_dev = nullptr;  // [max_pairs][6] warm-start motions (odo_batch_track_init)
     int last_n = 0, last_rgb = 0;  // pair count and photometric flag of the last tracking call
+    bool follow_legacy = true;     // stream NULL: order after the legacy default stream's work
+    cudaEvent_t order_ev = nullptr;
     std::map<GKey, cudaGraphExec_t> graphs;
     std::string last_error;
 };
@@ -459,6 +461,8 @@ int odo_batch_create(int max_pairs, odo_batch_t **out) {
     std::memset(b->args_host, 0, o);
     if ((e = cudaMalloc(&b->st_dev, sizeof(TrackState) * np)) != cudaSuccess) return bail(e, "cudaMalloc(states)");
     if ((e = cudaMalloc(&b->init_dev, sizeof(float) * 6 * np)) != cudaSuccess) return bail(e, "cudaMalloc(init)");
+    if ((e = cudaEventCreateWithFlags(&b->order_ev, cudaEventDisableTiming)) != cudaSuccess)
+        return bail(e, "cudaEventCreate");
     if ((e = cudaMallocHost(&b->st_host, sizeof(TrackState) * np)) != cudaSuccess)
         return bail(e, "cudaMallocHost(states)");
     *out = b;
@@ -475,6 +479,7 @@ int odo_batch_destroy(odo_batch_t *b) {
     if (b->st_dev) cudaFree(b->st_dev);
     if (b->st_host) cudaFreeHost(b->st_host);
     if (b->init_dev) cudaFree(b->init_dev);
+    if (b->order_ev) cudaEventDestroy(b->order_ev);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
     return ODO_OK;
@@ -488,6 +493,7 @@ int odo_batch_set_stream(odo_batch_t *b, void *stream) {
         drop_graphs(b);
         b->stream = s;
     }
+    b->follow_legacy = stream == nullptr;
     return ODO_OK;
 }
 
@@ -523,6 +529,10 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
     }
     const int warm = init != nullptr;
     if (warm) so3 = 0;
+    if (b->follow_legacy) {  // the inputs were produced on the legacy default stream
+        BCK(cudaEventRecord(b->order_ev, 0));
+        BCK(cudaStreamWaitEvent(b->stream, b->order_ev, 0));
+    }
     int rc = ensure_layout(b, pairs, npairs);
     if (rc != ODO_OK) return rc;
     const int rgb = rgbOnly || icpWeight < 100;

@@ -384,10 +384,9 @@ __global__ void k_transpose_bf16(const uint16_t *w, int rows, int cols, uint16_t
 // Network input of pair blockIdx.z: s x s block means of the valid depths
 // (metres; 0 where no pixel is valid) and of the intensities (the tracker's
 // weighting of the RGBA bytes, 0..1) of both frames, FP16; channels 4-7 are
-// derived from them in FP32 before rounding: 2 x (live - model intensity),
-// 4 x (live - model depth) clamped to +-0.25 m (0 unless both are valid),
-// and the valid-depth fractions of the two blocks (the differences keep the
-// precision that FP16 depth loses).
+// derived from them in FP32 before rounding: live - model intensity, live -
+// model depth (0 unless both are valid), and the valid-depth fractions of the
+// two blocks (the differences keep the precision that FP16 depth loses).
 __global__ void k_pack(const PackArgs *args, uint16_t *out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= kInW || y >= kInH) return;
@@ -427,10 +426,11 @@ __global__ void k_pack(const PackArgs *args, uint16_t *out) {
     h[1] = __float2half_rn(gm);
     h[2] = __float2half_rn(dl);
     h[3] = __float2half_rn(gl);
-    // differences scaled up (they are small) and the depth difference clamped
-    // to +-0.25 m (depth edges would otherwise give metre-sized outliers)
-    h[4] = __float2half_rn(2.f * (gl - gm));
-    h[5] = __float2half_rn((nm && nl) ? 4.f * fminf(0.25f, fmaxf(-0.25f, dl - dm)) : 0.f);
+    // unscaled and unclamped: the metre-sized depth differences at occlusion
+    // edges are part of the signal (clamping them to +-0.25 m, or dropping
+    // the derived channels, left the network unable to learn)
+    h[4] = __float2half_rn(gl - gm);
+    h[5] = __float2half_rn((nm && nl) ? dl - dm : 0.f);
     h[6] = __float2half_rn(nm * invn);
     h[7] = __float2half_rn(nl * invn);
     uint16_t *o = out + (((size_t)blockIdx.z * kInH + y) * kInW + x) * kInC;

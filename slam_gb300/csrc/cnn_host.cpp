@@ -200,7 +200,8 @@ int odo_cnn_destroy(odo_cnn_t *n) {
 
 int odo_cnn_set_stream(odo_cnn_t *n, void *stream) {
     if (!n) return ODO_ERR_ARG;
-    n->stream = stream ? (cudaStream_t)stream : n->own_stream;
+    // NULL: the legacy default stream itself (no graphs are captured here)
+    n->stream = stream ? (cudaStream_t)stream : cudaStreamLegacy;
     return ODO_OK;
 }
 

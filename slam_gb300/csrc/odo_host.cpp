@@ -69,6 +69,11 @@ struct odo_handle {
     float cx = 0, cy = 0, fx = 0, fy = 0, distThres = 0, angleThres = 0;
     int device = 0, sm_count = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
+    // set_stream(NULL): work runs on own_stream, ordered after the work
+    // already queued on the legacy default stream (where the caller's inputs
+    // were produced); graphs cannot be captured on the legacy stream itself
+    bool follow_legacy = true;
+    cudaEvent_t order_ev = nullptr;
     Arena arena;
     int dims_w[kLevels], dims_h[kLevels];
     DImg<uint16_t> depth_tmp[kLevels];
@@ -207,6 +212,15 @@ void default_launch(odo_t *h) {
     }
 }
 
+// Orders the handle's stream after the work queued on the legacy default
+// stream (see odo_handle::follow_legacy).
+cudaError_t follow_caller(odo_t *h) {
+    if (!h->follow_legacy) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(h->order_ev, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, h->order_ev, 0);
+    return e;
+}
+
 void drop_graphs(odo_t *h) {
     for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
@@ -307,6 +321,8 @@ int odo_create(int width, int height, float cx, float cy, float fx, float fy, fl
         return bail(e, "cudaDeviceGetAttribute");
     if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
         return bail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming)) != cudaSuccess)
+        return bail(e, "cudaEventCreate");
     h->stream = h->own_stream;
     for (int l = 0; l < kLevels; ++l) {
         int w = width >> l, hh = height >> l;
@@ -358,6 +374,7 @@ int odo_destroy(odo_t *h) {
     drop_graphs(h);
     h->arena.release();
     if (h->st_host) cudaFreeHost(h->st_host);
+    if (h->order_ev) cudaEventDestroy(h->order_ev);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return ODO_OK;
@@ -371,6 +388,7 @@ int odo_set_stream(odo_t *h, void *stream) {
         drop_graphs(h);
         h->stream = s;
     }
+    h->follow_legacy = stream == nullptr;
     return ODO_OK;
 }
 
@@ -390,6 +408,7 @@ int odo_set_precision(odo_t *h, int precision) {
 
 int odo_init_icp_depth(odo_t *h, const uint16_t *depth, size_t pitch_bytes, float depthCutoff) {
     if (!h || !depth || pitch_bytes < (size_t)h->width * 2) return ODO_ERR_ARG;
+    CK(follow_caller(h));
     cudaStream_t s = h->stream;
     CK(cudaMemcpy2DAsync(h->depth_tmp[0].data, h->depth_tmp[0].pitch, depth, pitch_bytes, (size_t)h->width * 2,
                          h->height, cudaMemcpyDeviceToDevice, s));
@@ -413,6 +432,7 @@ static int init_maps(odo_t *h, const float *verts, const float *norms, size_t pi
     if (!h || !verts || !norms || pitch_bytes < (size_t)h->width * 16 || (pitch_bytes % 16) != 0 ||
         ((uintptr_t)verts % 16) != 0 || ((uintptr_t)norms % 16) != 0)
         return ODO_ERR_ARG;
+    CK(follow_caller(h));
     Map3 v[kLevels], n[kLevels];
     for (int l = 0; l < kLevels; ++l) {
         v[l] = model ? h->vmap_prev[l].map() : h->vmap_curr[l].map();
@@ -460,22 +480,26 @@ static int populate(odo_t *h, const uint8_t *rgba, size_t pitch_bytes, DImg<floa
 
 int odo_init_rgb(odo_t *h, const uint8_t *rgba, size_t pitch_bytes) {
     if (!h) return ODO_ERR_ARG;
+    CK(follow_caller(h));
     return populate(h, rgba, pitch_bytes, h->nextDepth, h->nextImage());
 }
 
 int odo_init_rgb_model(odo_t *h, const uint8_t *rgba, size_t pitch_bytes) {
     if (!h) return ODO_ERR_ARG;
+    CK(follow_caller(h));
     return populate(h, rgba, pitch_bytes, h->lastDepth, h->lastImage);
 }
 
 int odo_init_first_rgb(odo_t *h, const uint8_t *rgba, size_t pitch_bytes) {
     if (!h) return ODO_ERR_ARG;
+    CK(follow_caller(h));
     return populate(h, rgba, pitch_bytes, nullptr, h->lastNextImage());
 }
 
 int odo_get_incremental_transformation(odo_t *h, float trans[3], float rot[9], int rgbOnly, float icpWeight,
                                        int pyramid, int fastOdom, int so3) {
     if (!h || !trans || !rot) return ODO_ERR_ARG;
+    CK(follow_caller(h));
     const int icp = !rgbOnly && icpWeight > 0;
     const int rgb = rgbOnly || icpWeight < 100;
     // src/odom/RGBDOdometryef.cpp:382-384

@@ -4,10 +4,9 @@ reference).
 A BF16 CNN proposes the SE(3) motion of a frame pair from both frames'
 160x120 depth and gray images; its forward and backward products run on the
 library's tcgen05 GEMM.  Inputs are CUDA tensors: [B, 120, 160, 8] float16
-(model depth m, model gray, live depth m, live gray, 2 x (live - model gray),
-4 x (live - model depth clamped to +-0.25 m), valid-depth fractions of both
-frames); outputs
-[B, 6] float32 (translation m, rotation vector rad).
+(model depth m, model gray, live depth m, live gray, live - model gray, live
+- model depth, valid-depth fractions of both frames); outputs [B, 6] float32
+(translation m, rotation vector rad).
 """
 import ctypes
 

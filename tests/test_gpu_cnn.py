@@ -142,3 +142,32 @@ def test_cnn_training_reduces_loss(gpu):
         last = net.train_step(xd, ld, 1e-3, want_loss=False)
     last = net.train_step(xd, ld, 1e-3)
     assert last < 0.1 * first, (first, last)
+
+
+def test_cnn_batch_consistency(gpu):
+    """Large batches (several 128-row tiles in every product): the outputs of
+    a batch equal those of its halves run alone, and the batch gradient is
+    the mean of the halves' gradients (the loss is a batch mean)."""
+    import torch
+    from slam_gb300.warmstart import WarmStartNet
+    net = WarmStartNet(max_batch=256, seed=5)
+    x, lab = _random_batch(256, 41)
+    xd = torch.from_numpy(x).cuda()
+    ld = torch.from_numpy(lab).cuda()
+    full = net.forward(xd).cpu().numpy()
+    lo = net.forward(xd[:128].contiguous()).cpu().numpy()
+    hi = net.forward(xd[128:].contiguous()).cpu().numpy()
+    scale = np.abs(full).max()
+    assert np.abs(full[:128] - lo).max() <= 1e-2 * scale
+    assert np.abs(full[128:] - hi).max() <= 1e-2 * scale
+    g, _ = net.gradients(xd, ld)
+    g1, _ = net.gradients(xd[:128].contiguous(), ld[:128].contiguous())
+    g2, _ = net.gradients(xd[128:].contiguous(), ld[128:].contiguous())
+    gm = 0.5 * (g1.astype(np.float64) + g2)
+    from oracle import oracle
+    w, b, total = oracle.cnn_layout()
+    for l in range(8):
+        for name, off, n in (("W", w[l], b[l] - w[l]), ("b", b[l], (w[l + 1] if l < 7 else total) - b[l])):
+            a, r = g[off:off + n].astype(np.float64), gm[off:off + n]
+            rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
+            assert rel < 3e-2, (l, name, rel)
