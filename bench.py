@@ -49,6 +49,12 @@ BYTES_PER_PX_ITER = 62  # ICP 48 B (4 maps x 12 B) + photometric 14 B per pixel-
 # + lastDepth 4 + lastImage 1 (the derivative images, 4 B, are read by the
 # photometric/solve kernel)
 PASS1_BYTES_PER_PX = 58
+# DRAM bytes (read + write) per pixel of the association kernel from ncu
+# captures on GB300 (profiles/k_icp_rgbres_b_L0_48pairs_640x480.md: 870.1 MB
+# for 48 x 307,200 px; profiles/k_icp_rgbres_L0_single_640x480.md: 17.1 MB
+# for 307,200 px); traffic grows with the pixels processed
+PASS1_TRAFFIC_PER_PX_BATCH = 870.1e6 / (48 * 307200)
+PASS1_TRAFFIC_PER_PX_SINGLE = 17.1e6 / 307200
 PREPROC_BYTES_PER_PX = 140  # per-frame map/pyramid building, per level-0 pixel (x 4/3 over the pyramid)
 
 
@@ -354,7 +360,7 @@ def run_ours(args):
                          "d2h_bytes_per_step": int(_native.load().odo_state_bytes())},
                  "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres (level 0)", "achieved": achieved,
                               "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                              "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
+                              "traffic": PASS1_TRAFFIC_PER_PX_SINGLE * n0, "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
                               "alg_bytes_per_launch": alg_bytes,
                               "note": "level-0 maps (~20 MB) are L2-resident within a frame"},
                  "frame_bytes": frame_bytes(cam, iters[1:]),
@@ -512,7 +518,9 @@ def measure_warm_batched(args, stream, local, world):
                     "d2h_bytes_per_step": int(nb * ctypes_sizeof_result())},
             "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres_b (level 0, all pairs of a step)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel_ms": k_ms, "photometric_kernel_ms": s_ms,
+                         "frac": achieved / peak, "traffic": PASS1_TRAFFIC_PER_PX_BATCH * px,
+                         "traffic_source": "ncu capture of 48 pairs scaled to the launch's pixels",
+                         "kernel_ms": k_ms, "photometric_kernel_ms": s_ms,
                          "iteration_ms": it_ms, "alg_bytes_per_launch": alg,
                          "alg_bytes_per_px": PASS1_BYTES_PER_PX},
             "plain_batched": {"frames_per_s": K * nb / (ms_p * 1e-3), "ms_per_step": ms_p / K,
@@ -841,10 +849,10 @@ def run_warm_study(args):
             if args.sweep:
                 rp0 = b.track(fps, descs=descs)
                 Pp0 = _res_array(rp0)[0]
-                for lv, it_ in ((1, (4, 0, 0)), (1, (6, 0, 0)), (2, (3, 3, 0)), (2, (5, 3, 0)), (3, (4, 3, 3)),
+                for lv, it_ in ((1, (4, 0, 0)), (2, (3, 3, 0)), (2, (4, 3, 0)), (3, (3, 3, 3)), (3, (4, 3, 3)),
                                 (3, (6, 4, 4))):
-                    for dis in (3.0, 5.0, 10.0):
-                        kw = dict(wkw, levels=lv, iterations=it_, max_disagree_deg=dis)
+                    for ratio in (1.5, 2.5, 4.0):
+                        kw = dict(wkw, levels=lv, iterations=it_, residual_limit=ratio * plain_res)
                         b.track_warm(net, fps, descs=descs, **kw)
                         torch.cuda.synchronize()
                         tt = time.perf_counter()
@@ -853,7 +861,7 @@ def run_warm_study(args):
                         tt = time.perf_counter() - tt
                         Pw0, ew0, _ = _res_array(rw0)
                         ee = _errs(Pw0, ps.T2)
-                        sweep.append({"levels": lv, "iterations": list(it_), "max_disagree_deg": dis,
+                        sweep.append({"levels": lv, "iterations": list(it_), "residual_ratio": ratio,
                                       "fps": m / tt, "fallback": float(fb0.mean()),
                                       "rot_p50": float(np.median(ee[:, 0])), "trans_p50": float(np.median(ee[:, 1])),
                                       "fail": float(np.mean((ee[:, 0] > np.radians(2)) | (ee[:, 1] > 0.05)))})
