@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-pairs", type=int, default=2000)
     ap.add_argument("--warm-levels", type=int, default=3)
-    ap.add_argument("--warm-iters", default="6,4,4")
+    ap.add_argument("--warm-iters", default="3,3,3")
     ap.add_argument("--max-disagree", type=float, default=5.0, help="warm study: fall-back angle (deg)")
     ap.add_argument("--oracle-pairs", type=int, default=24, help="warm study: pairs also tracked by the FP64 oracle")
     ap.add_argument("--save-params", default=None)
@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--sweep", action="store_true", help="warm study: also evaluate other warm schedules")
     ap.add_argument("--batch-pairs", type=int, default=500, help="pairs per warm-started batched step")
     ap.add_argument("--batch-steps", type=int, default=6, help="timed warm-started batched steps")
-    ap.add_argument("--residual-ratio", type=float, default=1.5)
+    ap.add_argument("--residual-ratio", type=float, default=4.0)
     a = ap.parse_args()
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
@@ -377,7 +377,8 @@ def run_ours(args):
                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": {"workload": f"warm-started batched tracking: {W['batch_pairs']} held-out 640x480 room pairs "
                                       "per step (6x4x3 m rooms, 20 spheres, motion <= 10 deg / 10 cm), network "
-                                      "proposal + 3 levels 6/4/4 without SO3, fall-back to the plain schedule",
+                                      f"proposal + {args.warm_levels} levels {args.warm_iters} without SO3, fall-back "
+                                      "to the plain schedule",
                           "batch_pairs": W["batch_pairs"], "warm_schedule": W["schedule"],
                           "fallback": W["fallback_cfg"], "train": W["train"], "launch": W["launch"],
                           "l2": f"inputs larger than L2: {W['pool_batches']} batches x {W['batch_bytes'] / 1e9:.1f} GB "
@@ -826,7 +827,7 @@ def run_warm_study(args):
         if args.save_params:
             np.savez(args.save_params, params=net.get_params(), plain_residual=plain_res, n_train=n_train)
     its = tuple(int(v) for v in args.warm_iters.split(","))
-    wkw = dict(levels=args.warm_levels, iterations=its, residual_limit=1.5 * plain_res,
+    wkw = dict(levels=args.warm_levels, iterations=its, residual_limit=args.residual_ratio * plain_res,
                max_disagree_deg=args.max_disagree)
     chunk, reps = 500, 3
     t_plain = t_warm = 0.0
@@ -936,7 +937,8 @@ def run_warm_study(args):
                       "train": {"pairs_rendered": args.train_pairs, "pairs_kept": n_train, "epochs": args.epochs,
                                 "generation_s": gen_s, "train_s": train_s, "last_epoch_loss": hist[-1]},
                       "warm_schedule": {"levels": args.warm_levels, "iterations": list(its), "so3": False},
-                      "fallback": {"residual_limit": 1.5 * plain_res, "max_disagree_deg": args.max_disagree}},
+                      "fallback": {"residual_limit": args.residual_ratio * plain_res, "residual_ratio": args.residual_ratio,
+                                   "max_disagree_deg": args.max_disagree}},
            "plain_batched_fps": n / (t_plain * 1e-3), "warm_batched_fps": n / (t_warm * 1e-3),
            "plain_single_pair_fps": single_fps,
            "speedup_vs_plain_batched": t_plain / t_warm, "speedup_vs_plain_single": n / (t_warm * 1e-3) / single_fps,
