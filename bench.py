@@ -78,11 +78,11 @@ def parse():
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
     ap.add_argument("--train-pairs", type=int, default=50000, help="warm study: rendered training pairs")
-    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-pairs", type=int, default=2000)
     ap.add_argument("--warm-levels", type=int, default=3)
-    ap.add_argument("--warm-iters", default="3,3,3")
+    ap.add_argument("--warm-iters", default="4,3,3")
     ap.add_argument("--max-disagree", type=float, default=5.0, help="warm study: fall-back angle (deg)")
     ap.add_argument("--oracle-pairs", type=int, default=24, help="warm study: pairs also tracked by the FP64 oracle")
     ap.add_argument("--save-params", default=None)
