@@ -45,15 +45,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ICP+RGB tracking frames/s @640x480: warm-started vs plain, equal pose error"
 BYTES_PER_PX_ITER = 62  # ICP 48 B (4 maps x 12 B) + photometric 14 B per pixel-iteration
-# the association/residual kernel's share: ICP 48 B + nextImage 1 + nextDepth 4
-# + lastDepth 4 + lastImage 1 (the derivative images, 4 B, are read by the
-# photometric/solve kernel)
-PASS1_BYTES_PER_PX = 58
+# the association/residual kernel's bytes: inputs 62 B (ICP maps 48 B +
+# nextImage 1 + nextDepth 4 + lastDepth 4 + lastImage 1 + dIdx/dIdy 4) and the
+# 16-byte correspondence record it writes for the photometric reduction
+# (which reads that record and nothing else)
+PASS1_BYTES_PER_PX = 62 + 16
 # DRAM bytes (read + write) per pixel of the association kernel from ncu
-# captures on GB300 (profiles/k_icp_rgbres_b_L0_48pairs_640x480.md: 870.1 MB
-# for 48 x 307,200 px; profiles/k_icp_rgbres_L0_single_640x480.md: 17.1 MB
-# for 307,200 px); traffic grows with the pixels processed
-PASS1_TRAFFIC_PER_PX_BATCH = 870.1e6 / (48 * 307200)
+# captures on GB300 (profiles/k_icp_rgbres_b_L0_48pairs_640x480.md: 826.9 MB
+# read + 223.8 MB written for 48 x 307,200 px;
+# profiles/k_icp_rgbres_L0_single_640x480.md: 17.1 MB for 307,200 px);
+# traffic grows with the pixels processed
+PASS1_TRAFFIC_PER_PX_BATCH = (826.9e6 + 223.8e6) / (48 * 307200)
 PASS1_TRAFFIC_PER_PX_SINGLE = 17.1e6 / 307200
 PREPROC_BYTES_PER_PX = 140  # per-frame map/pyramid building, per level-0 pixel (x 4/3 over the pyramid)
 
@@ -74,6 +76,7 @@ def parse():
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
+    ap.add_argument("--launch", default=None, help="batch study: fixed launch shape THREADSxPIXELS (e.g. 128x8)")
     ap.add_argument("--prefetch", action="store_true", help="enable the iteration kernels' L2 bulk prefetch")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
@@ -501,11 +504,11 @@ def measure_warm_batched(args, stream, local, world):
     fbr = float(np.mean(np.concatenate(fb_all)))
     # kernels per warm step: packing + 8 GEMMs per 256 pairs, the warm graph
     # (stamp, model maps, 2 photometric inputs, 4 pyramid steps, 2 depth
-    # pyramid steps, maps, derivatives, begin, seed, 2 per iteration, end) and
+    # pyramid steps, maps, derivatives, begin, seed, 3 per iteration, end) and
     # the fall-back batch with its SO3 stage
     gemm = -(-nb // 256) * 9
-    warm_graph = 13 + 2 * sum(its[:args.warm_levels])
-    plain_graph = 14 + 1 + 2 * 19
+    warm_graph = 13 + 3 * sum(its[:args.warm_levels])
+    plain_graph = 14 + 1 + 3 * 19
     launches = K * (gemm + warm_graph + (plain_graph if fbr > 0 else 0))
     return {"fps": K * nb / (ms_w * 1e-3), "ms_per_step": ms_w / K, "steps": K, "warmup": W, "batch_pairs": nb,
             "pool_batches": 2, "batch_bytes": batch_bytes,
@@ -582,7 +585,11 @@ def run_batch_study(args):
     b.track(fps)
     default_ms = (time.perf_counter() - t) * 1e3
     default_poses = [result_pose(r) for r in default_res]
-    if args.no_autotune:
+    if args.launch:
+        threads, ppt = (int(v) for v in args.launch.split("x"))
+        b.set_launch(threads, ppt)
+        tune_ms = None
+    elif args.no_autotune:
         threads, ppt, tune_ms = 256, 2, default_ms
     else:
         threads, ppt, tune_ms = b.autotune(fps)

@@ -194,7 +194,8 @@ int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOn
  * counterpart in the reference; used by the learned warm start). */
 int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init_dev, int rgbOnly,
                          float icpWeight, int fastOdom, odo_pair_result *results);
-/* Times every launch shape on these pairs, keeps the fastest and returns it. */
+/* Times every launch shape ({128, 256} threads x {2, 4, 8, 16, 32} pixels per
+ * thread) on these pairs, keeps the fastest and returns it. */
 int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
                        int so3, odo_pair_result *scratch_results, int *threads, int *pixels_per_thread,
                        float *best_ms);
@@ -209,7 +210,8 @@ int odo_batch_debug_time_iteration(odo_batch_t *b, int level, int reps, float ou
  * Buffer ids: 0 depth pyramid (u16), 1 vmap_curr, 2 nmap_curr, 3 vmap_prev,
  * 4 nmap_prev (planar float [3][rows][cols]), 5 lastDepth, 6 nextDepth
  * (float), 7 lastImage, 8 nextImage, 9 lastNextImage (u8), 10 dIdx, 11 dIdy
- * (int16), 12 correspondences (4 x int16 per pixel: u0, v0, diff, valid).
+ * (int16), 12 correspondences (16 bytes per pixel: int16 u0, v0, diff,
+ * valid; float model depth at (u0, v0); int16 dIdx, dIdy at the pixel).
  * Copies are dense (pitch = cols * element size) and synchronous. */
 int odo_debug_download(odo_t *h, int which, int level, void *host_dst, size_t bytes);
 int odo_debug_upload(odo_t *h, int which, int level, const void *host_src, size_t bytes);
@@ -262,6 +264,12 @@ int odo_debug_time_iteration(odo_t *h, int level, int reps, float out_ms[3]);
  * iteration kernels (default 0: measured slower); takes effect for calls made
  * afterwards (a handle's captured graphs keep the value they were built with). */
 int odo_debug_set_prefetch(int on);
+
+/* Process-wide switch of the batched tracker's last iteration stage: 1
+ * (default) the photometric pass and a one-block-per-pair solve kernel, 0 the
+ * single-pair layout (the solve in the last block of the photometric pass).
+ * Both give the same poses; takes effect for the next batch call. */
+int odo_batch_debug_set_split(int on);
 
 /* Device-side phase timers accumulated over tracking calls (ns):
  * out[0] last-block reduction of the block partials, out[1] FP64 solve and

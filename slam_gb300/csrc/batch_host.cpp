@@ -46,7 +46,7 @@ struct PairBufs {
 };
 
 using Layout = std::vector<std::tuple<int, int>>;
-using GKey = std::tuple<int, int, int, int, int, int, int, int, int>;
+using GKey = std::tuple<int, int, int, int, int, int, int, int, int, int>;
 
 }  // namespace
 
@@ -549,7 +549,8 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
     if (!graph) {
         BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters));
     } else {
-        GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt};
+        GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt,
+                 g_split_solve | (g_l2_prefetch << 1)};
         auto it = b->graphs.find(key);
         if (it == b->graphs.end()) {
             cudaGraph_t g = nullptr;
@@ -705,14 +706,14 @@ int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rg
                        float *best_ms) {
     if (!b || !threads || !pixels_per_thread) return ODO_ERR_ARG;
     const int cand_t[2] = {128, 256};
-    const int cand_p[4] = {1, 2, 4, 8};
+    const int cand_p[5] = {2, 4, 8, 16, 32};
     float best = 1e30f;
     int bt = b->threads, bp = b->ppt;
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
     for (int ti = 0; ti < 2; ++ti)
-        for (int pi = 0; pi < 4; ++pi) {
+        for (int pi = 0; pi < 5; ++pi) {
             int rc = odo_batch_set_launch(b, cand_t[ti], cand_p[pi]);
             if (rc == ODO_OK) rc = odo_batch_track(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3, scratch_results);
             if (rc != ODO_OK) {

@@ -278,7 +278,7 @@ int copy_level(odo_t *h, int which, int level, void *host, size_t bytes, bool up
         case 9: dptr = h->lastNextImage()[level].data; pitch = h->lastNextImage()[level].pitch; elem = 1; break;
         case 10: dptr = h->dIdx[level].data; pitch = h->dIdx[level].pitch; elem = 2; break;
         case 11: dptr = h->dIdy[level].data; pitch = h->dIdy[level].pitch; elem = 2; break;
-        case 12: dptr = h->corr[level].data; pitch = h->corr[level].pitch; elem = 8; break;
+        case 12: dptr = h->corr[level].data; pitch = h->corr[level].pitch; elem = 16; break;
         default: return ODO_ERR_ARG;
     }
     const size_t need = (size_t)cols * elem * rows;
@@ -701,6 +701,11 @@ int odo_debug_history(odo_t *h, double *out, int max_rows) {
 
 int odo_debug_set_prefetch(int on) {
     g_l2_prefetch = on ? 1 : 0;
+    return ODO_OK;
+}
+
+int odo_batch_debug_set_split(int on) {
+    g_split_solve = on ? 1 : 0;
     return ODO_OK;
 }
 

@@ -27,12 +27,18 @@ struct Map3 {
     int cols, rows;
 };
 
-// Photometric correspondence, 8 bytes: model pixel (u0, v0), intensity
-// difference, valid flag.  Replaces the 16-byte DataTerm
-// (src/cuda/types.cuh:75-81); the live pixel is implied by the position.
-struct Corr {
+// Photometric correspondence, 16 bytes, written by the residual pass and
+// read by the photometric reduction as one vector: model pixel (u0, v0),
+// intensity difference, valid flag, the model depth at (u0, v0) and the
+// live image derivatives at this pixel, so that the reduction gathers
+// nothing.  Replaces the 16-byte DataTerm (src/cuda/types.cuh:75-81); the
+// live pixel is implied by the position.
+struct __align__(16) Corr {
     int16_t u0, v0, diff, valid;
+    float z;
+    int16_t dx, dy;
 };
+static_assert(sizeof(Corr) == 16, "Corr layout");
 
 struct Intr {
     float fx, fy, cx, cy;
@@ -232,6 +238,8 @@ cudaError_t launch_level_iteration_batch(const PassArgs *args, int npairs, int m
 
 // process-wide switch of the iteration kernels' L2 bulk prefetch (default off)
 extern int g_l2_prefetch;
+// process-wide switch: batched photometric pass and solve as two kernels (default on)
+extern int g_split_solve;
 
 // debug single passes
 cudaError_t launch_debug_icp(const LevelArgs &L, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],

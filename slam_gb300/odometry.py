@@ -179,7 +179,7 @@ class RGBDOdometry:
         if which in (1, 2, 3, 4):
             return (3, h, w)
         if which == 12:
-            return (h, w, 4)
+            return (h, w, 8)  # int16 u0, v0, diff, valid, float z (2 slots), dIdx, dIdy
         return (h, w)
 
     def download(self, which, level):
