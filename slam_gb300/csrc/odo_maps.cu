@@ -16,38 +16,102 @@ namespace {
 
 constexpr int BX = 32, BY = 8;
 
-// pyrDownGaussKernel, src/odom/utils.cu:57-94 (sigma_color = 30, :103).
-__device__ __forceinline__ void pyr_px(const PyrArgs &a, int x, int y) {
+// Linear enumeration of the 32x8 tiles of all pyramid levels (level l is
+// (cols >> l) x (rows >> l)), so that a multi-level launch has no blocks for
+// pixels outside a level.
+struct LevelTiles {
+    int tx[kLevels];     // tiles per row of each level
+    int start[kLevels];  // first linear tile of each level
+    int total;
+};
+inline LevelTiles level_tiles(int cols, int rows, int nlevels) {
+    LevelTiles t{};
+    int s = 0;
+    for (int l = 0; l < kLevels; ++l) {
+        const int c = l < nlevels ? cols >> l : 0, r = l < nlevels ? rows >> l : 0;
+        t.tx[l] = (c + BX - 1) / BX;
+        t.start[l] = s;
+        s += t.tx[l] * ((r + BY - 1) / BY);
+    }
+    t.total = s;
+    return t;
+}
+__device__ __forceinline__ void tile_coords(const LevelTiles &t, int b, int &l, int &x, int &y) {
+    l = b >= t.start[2] ? 2 : (b >= t.start[1] ? 1 : 0);
+    const int k = b - t.start[l];
+    x = (k % t.tx[l]) * BX + threadIdx.x;
+    y = (k / t.tx[l]) * BY + threadIdx.y;
+}
+
+// The window kernels stage the source pixels of their 32x8 block in shared
+// memory (coalesced loads, each source pixel read once) and then run the
+// reference's window loops unchanged on the tile.  A 2x downsampling 5x5
+// window of the block's outputs covers source columns [2 X0 - 2, 2 X0 + 65)
+// and rows [2 Y0 - 2, 2 Y0 + 17); the same-level 3x3 / 4x4 windows of the
+// derivative kernel cover [X0 - 2, X0 + 33) x [Y0 - 2, Y0 + 9).  Tile
+// entries outside the image are never read (the loops clamp to the image).
+constexpr int kDownTW = 2 * BX + 4, kDownTH = 2 * BY + 4;
+constexpr int kDerTW = BX + 4, kDerTH = BY + 4;
+template <typename T, int TH, int TW>
+__device__ __forceinline__ void load_tile(const Img<const T> &src, int ox, int oy, T (&tile)[TH][TW]) {
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    for (int i = tid; i < TH * TW; i += nt) {
+        const int ty = i / TW, tx = i - ty * TW;
+        const int gx = ox + tx, gy = oy + ty;
+        if (gx >= 0 && gy >= 0 && gx < src.cols && gy < src.rows) tile[ty][tx] = at(src, gx, gy);
+    }
+}
+
+// pyrDownGaussKernel, src/odom/utils.cu:57-94 (sigma_color = 30, :103), on
+// a shared-memory tile of the source; (X0, Y0) = the block's first output.
+__device__ __forceinline__ void pyr_tile(const PyrArgs &a, int X0, int Y0) {
+    __shared__ uint16_t t[kDownTH][kDownTW];
     const Img<const uint16_t> src = a.src;
     const Img<uint16_t> dst = a.dst;
+    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
+    load_tile(src, ox, oy, t);
+    __syncthreads();
+    const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
     if (x >= dst.cols || y >= dst.rows) return;
     const int D = 5;
     const float sigma_color = 30.f;
-    int center = at(src, 2 * x, 2 * y);
+    int center = t[2 * y - oy][2 * x - ox];
     int x_mi = max(0, 2 * x - D / 2) - 2 * x;
     int y_mi = max(0, 2 * y - D / 2) - 2 * y;
     int x_ma = min(src.cols, 2 * x - D / 2 + D) - 2 * x;
     int y_ma = min(src.rows, 2 * y - D / 2 + D) - 2 * y;
     float sum = 0, wall = 0;
     const float weights[] = {0.375f, 0.25f, 0.0625f};
-    for (int yi = y_mi; yi < y_ma; ++yi) {
-        const uint16_t *r = rowp(src.data, src.pitch, 2 * y + yi);
-        for (int xi = x_mi; xi < x_ma; ++xi) {
-            int val = r[2 * x + xi];
-            if (abs(val - center) < 3 * sigma_color) {
-                sum += val * weights[abs(xi)] * weights[abs(yi)];
-                wall += weights[abs(xi)] * weights[abs(yi)];
+    if (x_mi == -2 && x_ma == 3 && y_mi == -2 && y_ma == 3) {
+        // interior: the same loop fully unrolled (weights become immediates)
+#pragma unroll
+        for (int yi = -2; yi < 3; ++yi) {
+            const uint16_t *r = t[2 * y + yi - oy] - ox;
+#pragma unroll
+            for (int xi = -2; xi < 3; ++xi) {
+                int val = r[2 * x + xi];
+                if (abs(val - center) < 3 * sigma_color) {
+                    sum += val * weights[xi < 0 ? -xi : xi] * weights[yi < 0 ? -yi : yi];
+                    wall += weights[xi < 0 ? -xi : xi] * weights[yi < 0 ? -yi : yi];
+                }
+            }
+        }
+    } else {
+        for (int yi = y_mi; yi < y_ma; ++yi) {
+            const uint16_t *r = t[2 * y + yi - oy] - ox;
+            for (int xi = x_mi; xi < x_ma; ++xi) {
+                int val = r[2 * x + xi];
+                if (abs(val - center) < 3 * sigma_color) {
+                    sum += val * weights[abs(xi)] * weights[abs(yi)];
+                    wall += weights[abs(xi)] * weights[abs(yi)];
+                }
             }
         }
     }
     at(dst, x, y) = static_cast<int>(sum / wall);
 }
-__global__ void k_pyr_down_depth(PyrArgs a) {
-    pyr_px(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
-}
-__global__ void k_pyr_down_depth_b(const PyrArgs *A) {
-    pyr_px(A[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
-}
+__global__ void k_pyr_down_depth(PyrArgs a) { pyr_tile(a, blockIdx.x * BX, blockIdx.y * BY); }
+__global__ void k_pyr_down_depth_b(const PyrArgs *A) { pyr_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * BY); }
 
 // computeVmapKernel, src/odom/utils.cu:109-133, for one pixel.
 __device__ __forceinline__ float3 vertex_at(const Img<const uint16_t> &depth, int u, int v, float fx_inv,
@@ -85,12 +149,15 @@ __device__ __forceinline__ void vnmap_px(const VNArgs &a, int l, int u, int v) {
     map_row(nm, 1, v)[u] = n.y;
     map_row(nm, 2, v)[u] = n.z;
 }
-__global__ void k_vmap_nmap(VNArgs a) {
-    vnmap_px(a, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+__global__ void k_vmap_nmap(VNArgs a, LevelTiles t) {
+    int l, x, y;
+    tile_coords(t, blockIdx.x, l, x, y);
+    vnmap_px(a, l, x, y);
 }
-__global__ void k_vmap_nmap_b(const VNArgs *A) {
-    vnmap_px(A[blockIdx.z / kLevels], blockIdx.z % kLevels, blockIdx.x * blockDim.x + threadIdx.x,
-             blockIdx.y * blockDim.y + threadIdx.y);
+__global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) {
+    int l, x, y;
+    tile_coords(t, blockIdx.x, l, x, y);
+    vnmap_px(A[blockIdx.z], l, x, y);
 }
 
 // copyMapsKernel (src/odom/utils.cu:270-310): a pixel is valid iff the
@@ -122,40 +189,12 @@ __device__ __forceinline__ float3 resize4(const float3 &a00, const float3 &a01, 
     return n;
 }
 
-__device__ __forceinline__ void level1_px(const ModelArgs &a, int x, int y, float3 &v, float3 &n) {
-    float3 v00, v01, v10, v11, n00, n01, n10, n11;
-    copy_px(a, 2 * x, 2 * y, v00, n00);
-    copy_px(a, 2 * x + 1, 2 * y, v01, n01);
-    copy_px(a, 2 * x, 2 * y + 1, v10, n10);
-    copy_px(a, 2 * x + 1, 2 * y + 1, v11, n11);
-    v = resize4<false>(v00, v01, v10, v11);
-    n = resize4<true>(n00, n01, n10, n11);
-}
 
-// initICPModel / initICP(maps) (src/odom/RGBDOdometryef.cpp:144-206):
-// copyMaps, resizeVMap/NMap x2 and tranformMaps for every level in one
-// launch (blockIdx.z = level); level l re-derives its 2^l x 2^l block from
-// the RGBA32F input with the reference's order of operations.
-__device__ __forceinline__ void model_px(const ModelArgs &a, int l, int x, int y) {
-    const Map3 vm = a.vmap[l], nm = a.nmap[l];
-    if (x >= vm.cols || y >= vm.rows) return;
-    float3 v, n;
-    if (l == 0) {
-        copy_px(a, x, y, v, n);
-        rowp(a.vz, a.vz_pitch, y)[x] = rowp(a.v4, a.pitch4, y)[4 * x + 2];
-    } else if (l == 1) {
-        level1_px(a, x, y, v, n);
-    } else {
-        float3 v00, v01, v10, v11, n00, n01, n10, n11;
-        level1_px(a, 2 * x, 2 * y, v00, n00);
-        level1_px(a, 2 * x + 1, 2 * y, v01, n01);
-        level1_px(a, 2 * x, 2 * y + 1, v10, n10);
-        level1_px(a, 2 * x + 1, 2 * y + 1, v11, n11);
-        v = resize4<false>(v00, v01, v10, v11);
-        n = resize4<true>(n00, n01, n10, n11);
-    }
+// tranformMapsKernel (src/odom/utils.cu:206-248) and the planar store of one
+// model-map pixel.
+__device__ __forceinline__ void store_model_px(const ModelArgs &a, const Map3 &vm, const Map3 &nm, int x, int y,
+                                               float3 v, float3 n) {
     if (a.do_transform) {
-        // tranformMapsKernel, src/odom/utils.cu:206-248
         const float q = qnan_f();
         float3 vd = make_float3(q, q, q), nd = make_float3(q, q, q);
         const M33 R = load_m33(a.R);
@@ -172,13 +211,54 @@ __device__ __forceinline__ void model_px(const ModelArgs &a, int l, int x, int y
     map_row(nm, 1, y)[x] = n.y;
     map_row(nm, 2, y)[x] = n.z;
 }
-__global__ void k_model_maps(ModelArgs a) {
-    model_px(a, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+
+__device__ __forceinline__ float3 shfl_xor3(float3 v, int m) {
+    return make_float3(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
+                       __shfl_xor_sync(0xffffffffu, v.z, m));
 }
-__global__ void k_model_maps_b(const ModelArgs *A) {
-    model_px(A[blockIdx.z / kLevels], blockIdx.z % kLevels, blockIdx.x * blockDim.x + threadIdx.x,
-             blockIdx.y * blockDim.y + threadIdx.y);
+
+// initICPModel / initICP(maps) (src/odom/RGBDOdometryef.cpp:144-206):
+// copyMaps, resizeVMap/NMap x2 and tranformMaps for every level, one 32x32
+// tile of the RGBA32F input per block of 16x16 threads, read once: thread
+// (tx, ty) imports the 2x2 level-0 pixels of its level-1 pixel and resizes
+// them; the level-2 pixel of a 2x2 thread quad (lanes l, l^1, l^16, l^17 of
+// one warp) is resized from the quad's untransformed level-1 values.  The
+// operations and their order are the reference's (copy, resize of the
+// untransformed level above, then the transform).
+constexpr int kModelTile = 32;  // level-0 pixels per tile side; block = 16 x 16 threads
+__device__ __forceinline__ void model_tile(const ModelArgs &a, int tile) {
+    const int tiles_x = (a.cols0 + kModelTile - 1) / kModelTile;
+    const int X1 = (tile % tiles_x) * (kModelTile / 2) + threadIdx.x;
+    const int Y1 = (tile / tiles_x) * (kModelTile / 2) + threadIdx.y;
+    const float q = qnan_f();
+    float3 v0[4], n0[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = 2 * X1 + (k & 1), y = 2 * Y1 + (k >> 1);
+        v0[k] = n0[k] = make_float3(q, q, q);
+        if (x < a.cols0 && y < a.rows0 && a.vmap[0].cols > 0) {
+            copy_px(a, x, y, v0[k], n0[k]);
+            rowp(a.vz, a.vz_pitch, y)[x] = rowp(a.v4, a.pitch4, y)[4 * x + 2];
+            store_model_px(a, a.vmap[0], a.nmap[0], x, y, v0[k], n0[k]);
+        }
+    }
+    const Map3 vm1 = a.vmap[1], nm1 = a.nmap[1];
+    const bool in1 = X1 < vm1.cols && Y1 < vm1.rows;
+    float3 v1 = make_float3(q, q, q), n1 = v1;
+    if (in1) {
+        v1 = resize4<false>(v0[0], v0[1], v0[2], v0[3]);
+        n1 = resize4<true>(n0[0], n0[1], n0[2], n0[3]);
+        store_model_px(a, vm1, nm1, X1, Y1, v1, n1);
+    }
+    const float3 v1x = shfl_xor3(v1, 1), v1y = shfl_xor3(v1, 16), v1xy = shfl_xor3(v1, 17);
+    const float3 n1x = shfl_xor3(n1, 1), n1y = shfl_xor3(n1, 16), n1xy = shfl_xor3(n1, 17);
+    const Map3 vm2 = a.vmap[2], nm2 = a.nmap[2];
+    const int X2 = X1 >> 1, Y2 = Y1 >> 1;
+    if (!(threadIdx.x & 1) && !(threadIdx.y & 1) && X2 < vm2.cols && Y2 < vm2.rows)
+        store_model_px(a, vm2, nm2, X2, Y2, resize4<false>(v1, v1x, v1y, v1xy), resize4<true>(n1, n1x, n1y, n1xy));
 }
+__global__ void __launch_bounds__(256) k_model_maps(ModelArgs a) { model_tile(a, blockIdx.x); }
+__global__ void __launch_bounds__(256) k_model_maps_b(const ModelArgs *A) { model_tile(A[blockIdx.z], blockIdx.x); }
 
 // verticesToDepthKernel (src/odom/utils.cu:526-537, cut at maxDepthRGB =
 // 6.0, src/odom/RGBDOdometryef.cpp:37) and bgr2IntensityKernel
@@ -207,26 +287,48 @@ __constant__ float c_gauss5x5[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36,
 // pyrDownKernelIntensityGauss (src/odom/utils.cu:470-500) in one launch:
 // masked 5x5 Gaussian, window clamped at cols-1/rows-1 (exclusive), reversed
 // kernel index, int count.
-__device__ __forceinline__ void gauss_px(const GaussArgs &a, int x, int y) {
-    const Img<const float> dsrc = a.dsrc;
+__device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
+    __shared__ float dt[kDownTH][kDownTW];
+    __shared__ uint8_t it[kDownTH][kDownTW];
     const Img<float> ddst = a.ddst;
     const Img<const uint8_t> isrc = a.isrc;
     const Img<uint8_t> idst = a.idst;
     const int do_depth = a.do_depth;
+    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
+    if (do_depth) load_tile(a.dsrc, ox, oy, dt);
+    load_tile(isrc, ox, oy, it);
+    __syncthreads();
+    const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
     if (x >= idst.cols || y >= idst.rows) return;
     const int D = 5;
     int tx = min(2 * x - D / 2 + D, isrc.cols - 1);
     int ty = min(2 * y - D / 2 + D, isrc.rows - 1);
     const int cy0 = max(0, 2 * y - D / 2), cx0 = max(0, 2 * x - D / 2);
+    // interior: the same loops fully unrolled (ty - cy - 1 = 4 - i, tx - cx - 1 = 4 - j)
+    const bool interior = cx0 == 2 * x - 2 && tx == 2 * x + 3 && cy0 == 2 * y - 2 && ty == 2 * y + 3;
     if (do_depth) {
         float sum = 0;
         int count = 0;
-        for (int cy = cy0; cy < ty; ++cy) {
-            const float *r = rowp(dsrc.data, dsrc.pitch, cy);
-            for (int cx = cx0; cx < tx; ++cx) {
-                if (!isnan(r[cx])) {
-                    sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
-                    count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+        if (interior) {
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                const float *r = dt[cy0 + i - oy] - ox + cx0;
+#pragma unroll
+                for (int j = 0; j < 5; ++j) {
+                    if (!isnan(r[j])) {
+                        sum += r[j] * c_gauss5x5[(4 - i) * 5 + (4 - j)];
+                        count += c_gauss5x5[(4 - i) * 5 + (4 - j)];
+                    }
+                }
+            }
+        } else {
+            for (int cy = cy0; cy < ty; ++cy) {
+                const float *r = dt[cy - oy] - ox;
+                for (int cx = cx0; cx < tx; ++cx) {
+                    if (!isnan(r[cx])) {
+                        sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+                        count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+                    }
                 }
             }
         }
@@ -235,24 +337,34 @@ __device__ __forceinline__ void gauss_px(const GaussArgs &a, int x, int y) {
     {
         float sum = 0;
         int count = 0;
-        for (int cy = cy0; cy < ty; ++cy) {
-            const uint8_t *r = rowp(isrc.data, isrc.pitch, cy);
-            for (int cx = cx0; cx < tx; ++cx) {
-                if (r[cx] > 0) {
-                    sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
-                    count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+        if (interior) {
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                const uint8_t *r = it[cy0 + i - oy] - ox + cx0;
+#pragma unroll
+                for (int j = 0; j < 5; ++j) {
+                    if (r[j] > 0) {
+                        sum += r[j] * c_gauss5x5[(4 - i) * 5 + (4 - j)];
+                        count += c_gauss5x5[(4 - i) * 5 + (4 - j)];
+                    }
+                }
+            }
+        } else {
+            for (int cy = cy0; cy < ty; ++cy) {
+                const uint8_t *r = it[cy - oy] - ox;
+                for (int cx = cx0; cx < tx; ++cx) {
+                    if (r[cx] > 0) {
+                        sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+                        count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+                    }
                 }
             }
         }
         at(idst, x, y) = (sum / (float)count);
     }
 }
-__global__ void k_gauss_down(GaussArgs a) {
-    gauss_px(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
-}
-__global__ void k_gauss_down_b(const GaussArgs *A) {
-    gauss_px(A[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
-}
+__global__ void k_gauss_down(GaussArgs a) { gauss_tile(a, blockIdx.x * BX, blockIdx.y * BY); }
+__global__ void k_gauss_down_b(const GaussArgs *A) { gauss_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * BY); }
 
 __constant__ float c_sobel_x[9] = {0.52201f, 0.00000f, -0.52201f, 0.79451f, -0.00000f,
                                    -0.79451f, 0.52201f, 0.00000f, -0.52201f};
@@ -266,16 +378,33 @@ __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.000
 // the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
 // into a byte mask, so the per-iteration pass reads one byte per pixel.
 __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, int x, int y) {
+    __shared__ uint8_t t[kDerTH][kDerTW];
     const Img<const uint8_t> src = a.src[l];
+    const int ox = x - (int)threadIdx.x - 2, oy = y - (int)threadIdx.y - 2;
+    load_tile(src, ox, oy, t);
+    __syncthreads();
     if (x >= src.cols || y >= src.rows) return;
     float dxVal = 0, dyVal = 0;
-    int kernelIndex = 8;
-    for (int j = max(y - 1, 0); j <= min(y + 1, src.rows - 1); j++) {
-        const uint8_t *r = rowp(src.data, src.pitch, j);
-        for (int i = max(x - 1, 0); i <= min(x + 1, src.cols - 1); i++) {
-            dxVal += (float)r[i] * c_sobel_x[kernelIndex];
-            dyVal += (float)r[i] * c_sobel_y[kernelIndex];
-            --kernelIndex;
+    if (x >= 1 && x <= src.cols - 2 && y >= 1 && y <= src.rows - 2) {
+        // interior: the same loop fully unrolled (kernelIndex = 8 - k)
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+            const uint8_t *r = t[y - 1 + jj - oy] - ox + x - 1;
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii) {
+                dxVal += (float)r[ii] * c_sobel_x[8 - (jj * 3 + ii)];
+                dyVal += (float)r[ii] * c_sobel_y[8 - (jj * 3 + ii)];
+            }
+        }
+    } else {
+        int kernelIndex = 8;
+        for (int j = max(y - 1, 0); j <= min(y + 1, src.rows - 1); j++) {
+            const uint8_t *r = t[j - oy] - ox;
+            for (int i = max(x - 1, 0); i <= min(x + 1, src.cols - 1); i++) {
+                dxVal += (float)r[i] * c_sobel_x[kernelIndex];
+                dyVal += (float)r[i] * c_sobel_y[kernelIndex];
+                --kernelIndex;
+            }
         }
     }
     const short sx = dxVal, sy = dyVal;
@@ -285,9 +414,18 @@ __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, int x, int y
     bool c = false;
     if (j0 < cols - 5 && i < rows - 1) {
         bool valid = true;
-        for (int u = max(i - 2, 0); u < min(i + 2, rows); u++) {
-            const uint8_t *r = rowp(src.data, src.pitch, u);
-            for (int v = max(j0 - 2, 0); v < min(j0 + 2, cols); v++) valid = valid && (r[v] > 0);
+        if (i >= 2 && j0 >= 2) {  // interior (i + 2 <= rows, j0 + 2 <= cols hold here)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint8_t *r = t[i - 2 + u - oy] - ox + j0 - 2;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) valid = valid && (r[v] > 0);
+            }
+        } else {
+            for (int u = max(i - 2, 0); u < min(i + 2, rows); u++) {
+                const uint8_t *r = t[u - oy] - ox;
+                for (int v = max(j0 - 2, 0); v < min(j0 + 2, cols); v++) valid = valid && (r[v] > 0);
+            }
         }
         if (valid) {
             float mTwo = (sx * sx) + (sy * sy);
@@ -296,12 +434,15 @@ __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, int x, int y
     }
     at(a.cand[l], x, y) = c ? 1 : 0;
 }
-__global__ void k_derivatives(DerivArgs a) {
-    deriv_px(a, blockIdx.z, threadIdx.x + blockIdx.x * blockDim.x, threadIdx.y + blockIdx.y * blockDim.y);
+__global__ void k_derivatives(DerivArgs a, LevelTiles t) {
+    int l, x, y;
+    tile_coords(t, blockIdx.x, l, x, y);
+    deriv_px(a, l, x, y);
 }
-__global__ void k_derivatives_b(const DerivArgs *A) {
-    deriv_px(A[blockIdx.z / kLevels], blockIdx.z % kLevels, threadIdx.x + blockIdx.x * blockDim.x,
-             threadIdx.y + blockIdx.y * blockDim.y);
+__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) {
+    int l, x, y;
+    tile_coords(t, blockIdx.x, l, x, y);
+    deriv_px(A[blockIdx.z], l, x, y);
 }
 
 inline dim3 grid2(int cols, int rows, int z = 1) { return dim3((cols + BX - 1) / BX, (rows + BY - 1) / BY, z); }
@@ -326,14 +467,15 @@ cudaError_t launch_vmap_nmap(const Img<const uint16_t> *depth, const Map3 *vmap,
         a.cy[l] = K[l].cy;
     }
     a.cutoff = cutoff;
-    k_vmap_nmap<<<grid2(depth[0].cols, depth[0].rows, nlevels), dim3(BX, BY), 0, s>>>(a);
+    const LevelTiles t = level_tiles(depth[0].cols, depth[0].rows, nlevels);
+    k_vmap_nmap<<<t.total, dim3(BX, BY), 0, s>>>(a, t);
     return cudaGetLastError();
 }
 
 cudaError_t launch_model_maps(const float *v4, const float *n4, size_t pitch4, int cols, int rows, const Map3 *vmap,
                               const Map3 *nmap, int nlevels, int do_transform, const float R[9], const float t[3],
                               float *vz, size_t vz_pitch, cudaStream_t s) {
-    ModelArgs a;
+    ModelArgs a{};
     a.v4 = v4;
     a.n4 = n4;
     a.pitch4 = pitch4;
@@ -348,7 +490,8 @@ cudaError_t launch_model_maps(const float *v4, const float *n4, size_t pitch4, i
     for (int i = 0; i < 3; ++i) a.t[i] = t[i];
     a.vz = vz;
     a.vz_pitch = vz_pitch;
-    k_model_maps<<<grid2(cols, rows, nlevels), dim3(BX, BY), 0, s>>>(a);
+    const int tiles = ((cols + kModelTile - 1) / kModelTile) * ((rows + kModelTile - 1) / kModelTile);
+    k_model_maps<<<tiles, dim3(kModelTile / 2, kModelTile / 2), 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -377,7 +520,8 @@ cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t>
         a.cand[l] = cand[l];
         a.minScale[l] = minScale[l];
     }
-    k_derivatives<<<grid2(src[0].cols, src[0].rows, nlevels), dim3(BX, BY), 0, s>>>(a);
+    const LevelTiles t = level_tiles(src[0].cols, src[0].rows, nlevels);
+    k_derivatives<<<t.total, dim3(BX, BY), 0, s>>>(a, t);
     return cudaGetLastError();
 }
 
@@ -386,11 +530,13 @@ cudaError_t launch_pyr_down_depth_batch(const PyrArgs *args, int npairs, int max
     return cudaGetLastError();
 }
 cudaError_t launch_vmap_nmap_batch(const VNArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_vmap_nmap_b<<<grid2(max_cols, max_rows, npairs * kLevels), dim3(BX, BY), 0, s>>>(args);
+    const LevelTiles t = level_tiles(max_cols, max_rows, kLevels);
+    k_vmap_nmap_b<<<dim3(t.total, 1, npairs), dim3(BX, BY), 0, s>>>(args, t);
     return cudaGetLastError();
 }
 cudaError_t launch_model_maps_batch(const ModelArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_model_maps_b<<<grid2(max_cols, max_rows, npairs * kLevels), dim3(BX, BY), 0, s>>>(args);
+    const int tiles = ((max_cols + kModelTile - 1) / kModelTile) * ((max_rows + kModelTile - 1) / kModelTile);
+    k_model_maps_b<<<dim3(tiles, 1, npairs), dim3(kModelTile / 2, kModelTile / 2), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_rgbd_level0_batch(const RgbdArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
@@ -402,7 +548,8 @@ cudaError_t launch_gauss_down_batch(const GaussArgs *args, int npairs, int max_c
     return cudaGetLastError();
 }
 cudaError_t launch_derivatives_batch(const DerivArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_derivatives_b<<<grid2(max_cols, max_rows, npairs * kLevels), dim3(BX, BY), 0, s>>>(args);
+    const LevelTiles t = level_tiles(max_cols, max_rows, kLevels);
+    k_derivatives_b<<<dim3(t.total, 1, npairs), dim3(BX, BY), 0, s>>>(args, t);
     return cudaGetLastError();
 }
 
