@@ -5,7 +5,7 @@ Headline (value): warm-started batched tracking.  A step = one batch of
 --batch-pairs held-out 640x480 frame pairs (6x4x3 m rooms with 20 spheres,
 fx = fy = 525, depth noise 0.0012 z^2, 5 % dropout, relative motion <= 10 deg /
 10 cm) tracked by one odo_batch_track_warm call: the warm-start network's
-proposal for every pair, 3 pyramid levels with 4/3/3 ICP+RGB iterations and
+proposal for every pair, 3 pyramid levels with 3/2/2 ICP+RGB iterations and
 no SO3 stage, and a fall-back to the reference's schedule (SO3 + 10/5/4) for
 the pairs whose residual or proposal disagreement fails the test.  The
 network is trained first, on the GPU, by the library's own kernels, on
@@ -81,12 +81,12 @@ def parse():
     ap.add_argument("--prefetch", action="store_true", help="enable the iteration kernels' L2 bulk prefetch")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
-    ap.add_argument("--train-pairs", type=int, default=50000, help="warm study: rendered training pairs")
-    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--train-pairs", type=int, default=100000, help="warm study: rendered training pairs")
+    ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-pairs", type=int, default=2000)
     ap.add_argument("--warm-levels", type=int, default=3)
-    ap.add_argument("--warm-iters", default="4,3,3")
+    ap.add_argument("--warm-iters", default="3,2,2")
     ap.add_argument("--max-disagree", type=float, default=5.0, help="warm study: fall-back angle (deg)")
     ap.add_argument("--oracle-pairs", type=int, default=24, help="warm study: pairs also tracked by the FP64 oracle")
     ap.add_argument("--save-params", default=None)
@@ -94,7 +94,7 @@ def parse():
     ap.add_argument("--sweep", action="store_true", help="warm study: also evaluate other warm schedules")
     ap.add_argument("--batch-pairs", type=int, default=500, help="pairs per warm-started batched step")
     ap.add_argument("--batch-steps", type=int, default=6, help="timed warm-started batched steps")
-    ap.add_argument("--residual-ratio", type=float, default=4.0)
+    ap.add_argument("--residual-ratio", type=float, default=6.0)
     a = ap.parse_args()
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
