@@ -16,9 +16,11 @@ namespace {
 
 constexpr int BX = 32, BY = 8;
 
-// Linear enumeration of the 32x8 tiles of all pyramid levels (level l is
-// (cols >> l) x (rows >> l)), so that a multi-level launch has no blocks for
-// pixels outside a level.
+// Linear enumeration of the 32 x kTileRows tiles of all pyramid levels
+// (level l is (cols >> l) x (rows >> l)), so that a multi-level launch has no
+// blocks for pixels outside a level; a 32x8 block covers a tile in
+// kTileRows / 8 passes.
+constexpr int kTileRows = 32;
 struct LevelTiles {
     int tx[kLevels];     // tiles per row of each level
     int start[kLevels];  // first linear tile of each level
@@ -31,47 +33,58 @@ inline LevelTiles level_tiles(int cols, int rows, int nlevels) {
         const int c = l < nlevels ? cols >> l : 0, r = l < nlevels ? rows >> l : 0;
         t.tx[l] = (c + BX - 1) / BX;
         t.start[l] = s;
-        s += t.tx[l] * ((r + BY - 1) / BY);
+        s += t.tx[l] * ((r + kTileRows - 1) / kTileRows);
     }
     t.total = s;
     return t;
 }
-__device__ __forceinline__ void tile_coords(const LevelTiles &t, int b, int &l, int &x, int &y) {
+// Level and first pixel (X0, Y0) of linear tile b.
+__device__ __forceinline__ void tile_origin(const LevelTiles &t, int b, int &l, int &X0, int &Y0) {
     l = b >= t.start[2] ? 2 : (b >= t.start[1] ? 1 : 0);
     const int k = b - t.start[l];
-    x = (k % t.tx[l]) * BX + threadIdx.x;
-    y = (k / t.tx[l]) * BY + threadIdx.y;
+    X0 = (k % t.tx[l]) * BX;
+    Y0 = (k / t.tx[l]) * kTileRows;
 }
 
 // The window kernels stage the source pixels of their 32x8 block in shared
 // memory (coalesced loads, each source pixel read once) and then run the
 // reference's window loops unchanged on the tile.  A 2x downsampling 5x5
-// window of the block's outputs covers source columns [2 X0 - 2, 2 X0 + 65)
-// and rows [2 Y0 - 2, 2 Y0 + 17); the same-level 3x3 / 4x4 windows of the
-// derivative kernel cover [X0 - 2, X0 + 33) x [Y0 - 2, Y0 + 9).  Tile
-// entries outside the image are never read (the loops clamp to the image).
-constexpr int kDownTW = 2 * BX + 4, kDownTH = 2 * BY + 4;
-constexpr int kDerTW = BX + 4, kDerTH = BY + 4;
+// window of the block's 32 x 32 outputs covers source columns
+// [2 X0 - 2, 2 X0 + 65) and rows [2 Y0 - 2, 2 Y0 + 65); the same-level 3x3 /
+// 4x4 windows of the derivative kernel cover [X0 - 2, X0 + 33) x
+// [Y0 - 2, Y0 + 33).  Each thread computes four outputs (rows 8 apart), so a
+// block's load round trip is shared by 1024 outputs.  Tile entries outside
+// the image are never read (the loops clamp to the image).
+constexpr int kDownTW = 2 * BX + 4, kDownTH = 2 * kTileRows + 4;
+constexpr int kDerTW = BX + 4, kDerTH = kTileRows + 4;
+// All loads of a thread are issued before the first store to shared memory
+// (a register array of compile-time size), so a block waits for one memory
+// round trip, not one per element.  Blocks are BX x BY threads.
 template <typename T, int TH, int TW>
 __device__ __forceinline__ void load_tile(const Img<const T> &src, int ox, int oy, T (&tile)[TH][TW]) {
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int i = tid; i < TH * TW; i += nt) {
+    constexpr int N = TH * TW, NT = BX * BY, IT = (N + NT - 1) / NT;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    T v[IT];
+#pragma unroll
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
         const int ty = i / TW, tx = i - ty * TW;
         const int gx = ox + tx, gy = oy + ty;
-        if (gx >= 0 && gy >= 0 && gx < src.cols && gy < src.rows) tile[ty][tx] = at(src, gx, gy);
+        v[k] = T{};
+        if (i < N && gx >= 0 && gy >= 0 && gx < src.cols && gy < src.rows) v[k] = at(src, gx, gy);
     }
+    T *flat = &tile[0][0];
+#pragma unroll
+    for (int k = 0; k < IT; ++k)
+        if (tid + k * NT < N) flat[tid + k * NT] = v[k];
 }
 
 // pyrDownGaussKernel, src/odom/utils.cu:57-94 (sigma_color = 30, :103), on
 // a shared-memory tile of the source; (X0, Y0) = the block's first output.
-__device__ __forceinline__ void pyr_tile(const PyrArgs &a, int X0, int Y0) {
-    __shared__ uint16_t t[kDownTH][kDownTW];
+__device__ __forceinline__ void pyr_out(const PyrArgs &a, const uint16_t (&t)[kDownTH][kDownTW], int ox, int oy,
+                                        int x, int y) {
     const Img<const uint16_t> src = a.src;
     const Img<uint16_t> dst = a.dst;
-    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
-    load_tile(src, ox, oy, t);
-    __syncthreads();
-    const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
     if (x >= dst.cols || y >= dst.rows) return;
     const int D = 5;
     const float sigma_color = 30.f;
@@ -90,7 +103,7 @@ __device__ __forceinline__ void pyr_tile(const PyrArgs &a, int X0, int Y0) {
 #pragma unroll
             for (int xi = -2; xi < 3; ++xi) {
                 int val = r[2 * x + xi];
-                if (abs(val - center) < 3 * sigma_color) {
+                if (abs(val - center) < 90) {  // 3 * sigma_color = 90.0f exactly
                     sum += val * weights[xi < 0 ? -xi : xi] * weights[yi < 0 ? -yi : yi];
                     wall += weights[xi < 0 ? -xi : xi] * weights[yi < 0 ? -yi : yi];
                 }
@@ -110,8 +123,16 @@ __device__ __forceinline__ void pyr_tile(const PyrArgs &a, int X0, int Y0) {
     }
     at(dst, x, y) = static_cast<int>(sum / wall);
 }
-__global__ void k_pyr_down_depth(PyrArgs a) { pyr_tile(a, blockIdx.x * BX, blockIdx.y * BY); }
-__global__ void k_pyr_down_depth_b(const PyrArgs *A) { pyr_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * BY); }
+__device__ __forceinline__ void pyr_tile(const PyrArgs &a, int X0, int Y0) {
+    __shared__ uint16_t t[kDownTH][kDownTW];
+    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
+    load_tile(a.src, ox, oy, t);
+    __syncthreads();
+#pragma unroll 1
+    for (int r = 0; r < kTileRows / BY; ++r) pyr_out(a, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+}
+__global__ void k_pyr_down_depth(PyrArgs a) { pyr_tile(a, blockIdx.x * BX, blockIdx.y * kTileRows); }
+__global__ void k_pyr_down_depth_b(const PyrArgs *A) { pyr_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRows); }
 
 // computeVmapKernel, src/odom/utils.cu:109-133, for one pixel.
 __device__ __forceinline__ float3 vertex_at(const Img<const uint16_t> &depth, int u, int v, float fx_inv,
@@ -149,16 +170,14 @@ __device__ __forceinline__ void vnmap_px(const VNArgs &a, int l, int u, int v) {
     map_row(nm, 1, v)[u] = n.y;
     map_row(nm, 2, v)[u] = n.z;
 }
-__global__ void k_vmap_nmap(VNArgs a, LevelTiles t) {
-    int l, x, y;
-    tile_coords(t, blockIdx.x, l, x, y);
-    vnmap_px(a, l, x, y);
+__device__ __forceinline__ void vnmap_tile(const VNArgs &a, const LevelTiles &t) {
+    int l, X0, Y0;
+    tile_origin(t, blockIdx.x, l, X0, Y0);
+#pragma unroll 1
+    for (int r = 0; r < kTileRows / BY; ++r) vnmap_px(a, l, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
-__global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) {
-    int l, x, y;
-    tile_coords(t, blockIdx.x, l, x, y);
-    vnmap_px(A[blockIdx.z], l, x, y);
-}
+__global__ void k_vmap_nmap(VNArgs a, LevelTiles t) { vnmap_tile(a, t); }
+__global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) { vnmap_tile(A[blockIdx.z], t); }
 
 // copyMapsKernel (src/odom/utils.cu:270-310): a pixel is valid iff the
 // vertex z != 0.
@@ -274,31 +293,64 @@ __device__ __forceinline__ void rgbd_px(const RgbdArgs &a, int x, int y) {
     int value = (float)src.x * 0.114f + (float)src.y * 0.299f + (float)src.z * 0.587f;
     at(a.img0, x, y) = value;
 }
+// Four consecutive pixels per thread: 16-byte loads of the vertex z and the
+// RGBA bytes and 16 / 4-byte stores when the rows allow it (the library's
+// buffers always do; the caller's RGBA image needs a 16-byte aligned base and
+// pitch), else the same pixels one by one.
+__device__ __forceinline__ void rgbd_px4(const RgbdArgs &a, int x0, int y) {
+    const int cols = a.img0.cols;
+    if (x0 >= cols || y >= a.img0.rows) return;
+    const bool vec = x0 + 3 < cols &&
+                     !(((uintptr_t)a.rgba | (uintptr_t)a.rgba_pitch | (uintptr_t)a.vz | (uintptr_t)a.vz_pitch) & 15);
+    if (!vec) {
+        for (int k = 0; k < 4 && x0 + k < cols; ++k) rgbd_px(a, x0 + k, y);
+        return;
+    }
+    const uint4 c4 = *reinterpret_cast<const uint4 *>(rowp(a.rgba, a.rgba_pitch, y) + 4 * x0);
+    const unsigned cw[4] = {c4.x, c4.y, c4.z, c4.w};
+    unsigned packed = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float r = (float)(cw[k] & 0xff), g = (float)((cw[k] >> 8) & 0xff), b = (float)((cw[k] >> 16) & 0xff);
+        int value = r * 0.114f + g * 0.299f + b * 0.587f;
+        packed |= ((unsigned)value & 0xffu) << (8 * k);
+    }
+    *reinterpret_cast<unsigned *>(&at(a.img0, x0, y)) = packed;
+    if (a.do_depth) {
+        const float cutOff = 6.0f;
+        const float4 z4 = *reinterpret_cast<const float4 *>(rowp(a.vz, a.vz_pitch, y) + x0);
+        const float zs[4] = {z4.x, z4.y, z4.z, z4.w};
+        float d[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) d[k] = zs[k] > cutOff || zs[k] <= 0 ? qnan_f() : zs[k];
+        *reinterpret_cast<float4 *>(&at(a.depth0, x0, y)) = make_float4(d[0], d[1], d[2], d[3]);
+    }
+}
 __global__ void k_rgbd_level0(RgbdArgs a) {
-    rgbd_px(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+    rgbd_px4(a, 4 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y * blockDim.y + threadIdx.y);
 }
 __global__ void k_rgbd_level0_b(const RgbdArgs *A) {
-    rgbd_px(A[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+    rgbd_px4(A[blockIdx.z], 4 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 __constant__ float c_gauss5x5[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36, 24, 6, 4, 16, 24, 16, 4, 1, 4, 6, 4, 1};
+// The same weights as compile-time integers for the unrolled interior loops
+// (the reference's `count += weight` on an int: all weights and partial
+// counts are small integers, so integer addition gives the same value).
+__host__ __device__ constexpr int gauss_w(int i, int j) {
+    return (i == 0 || i == 4 ? 1 : (i == 2 ? 6 : 4)) * (j == 0 || j == 4 ? 1 : (j == 2 ? 6 : 4));
+}
 
 // pyrDownKernelGaussF (src/odom/utils.cu:332-363) and
 // pyrDownKernelIntensityGauss (src/odom/utils.cu:470-500) in one launch:
 // masked 5x5 Gaussian, window clamped at cols-1/rows-1 (exclusive), reversed
 // kernel index, int count.
-__device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
-    __shared__ float dt[kDownTH][kDownTW];
-    __shared__ uint8_t it[kDownTH][kDownTW];
+__device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[kDownTH][kDownTW],
+                                          const uint8_t (&it)[kDownTH][kDownTW], int ox, int oy, int x, int y) {
     const Img<float> ddst = a.ddst;
     const Img<const uint8_t> isrc = a.isrc;
     const Img<uint8_t> idst = a.idst;
     const int do_depth = a.do_depth;
-    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
-    if (do_depth) load_tile(a.dsrc, ox, oy, dt);
-    load_tile(isrc, ox, oy, it);
-    __syncthreads();
-    const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
     if (x >= idst.cols || y >= idst.rows) return;
     const int D = 5;
     int tx = min(2 * x - D / 2 + D, isrc.cols - 1);
@@ -316,8 +368,8 @@ __device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
                     if (!isnan(r[j])) {
-                        sum += r[j] * c_gauss5x5[(4 - i) * 5 + (4 - j)];
-                        count += c_gauss5x5[(4 - i) * 5 + (4 - j)];
+                        sum += r[j] * (float)gauss_w(4 - i, 4 - j);
+                        count += gauss_w(4 - i, 4 - j);
                     }
                 }
             }
@@ -344,8 +396,8 @@ __device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
                     if (r[j] > 0) {
-                        sum += r[j] * c_gauss5x5[(4 - i) * 5 + (4 - j)];
-                        count += c_gauss5x5[(4 - i) * 5 + (4 - j)];
+                        sum += r[j] * (float)gauss_w(4 - i, 4 - j);
+                        count += gauss_w(4 - i, 4 - j);
                     }
                 }
             }
@@ -363,8 +415,18 @@ __device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
         at(idst, x, y) = (sum / (float)count);
     }
 }
-__global__ void k_gauss_down(GaussArgs a) { gauss_tile(a, blockIdx.x * BX, blockIdx.y * BY); }
-__global__ void k_gauss_down_b(const GaussArgs *A) { gauss_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * BY); }
+__device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
+    __shared__ float dt[kDownTH][kDownTW];
+    __shared__ uint8_t it[kDownTH][kDownTW];
+    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
+    if (a.do_depth) load_tile(a.dsrc, ox, oy, dt);
+    load_tile(a.isrc, ox, oy, it);
+    __syncthreads();
+#pragma unroll 1
+    for (int r = 0; r < kTileRows / BY; ++r) gauss_out(a, dt, it, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+}
+__global__ void k_gauss_down(GaussArgs a) { gauss_tile(a, blockIdx.x * BX, blockIdx.y * kTileRows); }
+__global__ void k_gauss_down_b(const GaussArgs *A) { gauss_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRows); }
 
 __constant__ float c_sobel_x[9] = {0.52201f, 0.00000f, -0.52201f, 0.79451f, -0.00000f,
                                    -0.79451f, 0.52201f, 0.00000f, -0.52201f};
@@ -377,12 +439,9 @@ __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.000
 // src/odom/reduce.cu:782-810: j0 < cols-5, i < rows-1, no zero intensity in
 // the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
 // into a byte mask, so the per-iteration pass reads one byte per pixel.
-__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, int x, int y) {
-    __shared__ uint8_t t[kDerTH][kDerTW];
+__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_t (&t)[kDerTH][kDerTW], int ox,
+                                         int oy, int x, int y) {
     const Img<const uint8_t> src = a.src[l];
-    const int ox = x - (int)threadIdx.x - 2, oy = y - (int)threadIdx.y - 2;
-    load_tile(src, ox, oy, t);
-    __syncthreads();
     if (x >= src.cols || y >= src.rows) return;
     float dxVal = 0, dyVal = 0;
     if (x >= 1 && x <= src.cols - 2 && y >= 1 && y <= src.rows - 2) {
@@ -434,23 +493,29 @@ __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, int x, int y
     }
     at(a.cand[l], x, y) = c ? 1 : 0;
 }
-__global__ void k_derivatives(DerivArgs a, LevelTiles t) {
-    int l, x, y;
-    tile_coords(t, blockIdx.x, l, x, y);
-    deriv_px(a, l, x, y);
+__device__ __forceinline__ void deriv_tile(const DerivArgs &a, const LevelTiles &lt) {
+    __shared__ uint8_t t[kDerTH][kDerTW];
+    int l, X0, Y0;
+    tile_origin(lt, blockIdx.x, l, X0, Y0);
+    const int ox = X0 - 2, oy = Y0 - 2;
+    load_tile(a.src[l], ox, oy, t);
+    __syncthreads();
+#pragma unroll 1
+    for (int r = 0; r < kTileRows / BY; ++r) deriv_px(a, l, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
-__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) {
-    int l, x, y;
-    tile_coords(t, blockIdx.x, l, x, y);
-    deriv_px(A[blockIdx.z], l, x, y);
-}
+__global__ void k_derivatives(DerivArgs a, LevelTiles t) { deriv_tile(a, t); }
+__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) { deriv_tile(A[blockIdx.z], t); }
 
 inline dim3 grid2(int cols, int rows, int z = 1) { return dim3((cols + BX - 1) / BX, (rows + BY - 1) / BY, z); }
+// grid of the window kernels: 32 x kTileRows outputs per block
+inline dim3 grid_tall(int cols, int rows, int z = 1) {
+    return dim3((cols + BX - 1) / BX, (rows + kTileRows - 1) / kTileRows, z);
+}
 
 }  // namespace
 
 cudaError_t launch_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst, cudaStream_t s) {
-    k_pyr_down_depth<<<grid2(dst.cols, dst.rows), dim3(BX, BY), 0, s>>>(PyrArgs{src, dst});
+    k_pyr_down_depth<<<grid_tall(dst.cols, dst.rows), dim3(BX, BY), 0, s>>>(PyrArgs{src, dst});
     return cudaGetLastError();
 }
 
@@ -497,14 +562,14 @@ cudaError_t launch_model_maps(const float *v4, const float *n4, size_t pitch4, i
 
 cudaError_t launch_rgbd_level0(const float *vz, size_t vz_pitch, const uint8_t *rgba, size_t rgba_pitch, int cols,
                                int rows, Img<float> depth0, Img<uint8_t> img0, int do_depth, cudaStream_t s) {
-    k_rgbd_level0<<<grid2(cols, rows), dim3(BX, BY), 0, s>>>(
+    k_rgbd_level0<<<grid2((cols + 3) / 4, rows), dim3(BX, BY), 0, s>>>(
         RgbdArgs{vz, vz_pitch, rgba, rgba_pitch, depth0, img0, do_depth});
     return cudaGetLastError();
 }
 
 cudaError_t launch_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const uint8_t> isrc, Img<uint8_t> idst,
                               int do_depth, cudaStream_t s) {
-    k_gauss_down<<<grid2(idst.cols, idst.rows), dim3(BX, BY), 0, s>>>(GaussArgs{dsrc, ddst, isrc, idst, do_depth});
+    k_gauss_down<<<grid_tall(idst.cols, idst.rows), dim3(BX, BY), 0, s>>>(GaussArgs{dsrc, ddst, isrc, idst, do_depth});
     return cudaGetLastError();
 }
 
@@ -526,7 +591,7 @@ cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t>
 }
 
 cudaError_t launch_pyr_down_depth_batch(const PyrArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_pyr_down_depth_b<<<grid2(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    k_pyr_down_depth_b<<<grid_tall(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_vmap_nmap_batch(const VNArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
@@ -540,11 +605,11 @@ cudaError_t launch_model_maps_batch(const ModelArgs *args, int npairs, int max_c
     return cudaGetLastError();
 }
 cudaError_t launch_rgbd_level0_batch(const RgbdArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_rgbd_level0_b<<<grid2(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    k_rgbd_level0_b<<<grid2((max_cols + 3) / 4, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_gauss_down_batch(const GaussArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_gauss_down_b<<<grid2(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    k_gauss_down_b<<<grid_tall(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_derivatives_batch(const DerivArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
