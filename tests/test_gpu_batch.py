@@ -70,4 +70,29 @@ def test_batch_autotune_runs(gpu):
     pairs = make_pairs(4, seed=3)
     b = BatchOdometry(4)
     t, ppt, ms = b.autotune(to_batch(pairs))
-    assert t in (128, 256) and ppt in (1, 2, 4, 8) and ms > 0
+    assert t in (128, 256) and ppt in (2, 4, 8, 16, 32) and ms > 0
+
+
+@pytest.mark.parametrize("launch", [(256, 2), (128, 32)], ids=["256x2", "128x32"])
+def test_batch_split_solve_matches_fused(gpu, launch):
+    """The batched iteration as three kernels (photometric pass, then one
+    solve block per pair) gives the same bits as the single-pair layout
+    (the solve in the last block of the photometric pass)."""
+    from slam_gb300 import _native
+    from slam_gb300.batch import BatchOdometry, result_pose
+    L = _native.load()
+    pairs = make_pairs(6, seed=11)
+    fp = to_batch(pairs)
+    out = []
+    try:
+        for split in (1, 0):
+            L.odo_batch_debug_set_split(split)
+            b = BatchOdometry(8)
+            b.set_launch(*launch)
+            res = b.track(fp)
+            out.append(([result_pose(r) for r in res], [list(r.iterations) for r in res]))
+    finally:
+        L.odo_batch_debug_set_split(1)
+    for i in range(len(pairs)):
+        assert np.array_equal(out[0][0][i], out[1][0][i]), i
+        assert out[0][1][i] == out[1][1][i]
