@@ -12,8 +12,10 @@ constexpr int kLevels = 3;
 
 // Pitched 2-D image view (pitch in bytes), like the reference's
 // PtrStepSz<T> (src/cuda/containers/kernel_containers.hpp:72-92).
+// 16-byte aligned so that a kernel holding the descriptor in shared memory
+// reads {data, pitch} with one 16-byte load.
 template <typename T>
-struct Img {
+struct __align__(16) Img {
     T *data;
     size_t pitch;
     int cols, rows;
@@ -21,7 +23,7 @@ struct Img {
 
 // Planar 3-channel map [3][rows][cols] with a row pitch in bytes (the
 // reference's DeviceArray2D<float>(rows*3, cols), src/odom/RGBDOdometryef.cpp:97-101).
-struct Map3 {
+struct __align__(16) Map3 {
     float *data;
     size_t pitch;
     int cols, rows;
