@@ -96,19 +96,25 @@ __device__ __forceinline__ void pyr_out(const PyrArgs &a, const uint16_t (&t)[kD
     float sum = 0, wall = 0;
     const float weights[] = {0.375f, 0.25f, 0.0625f};
     if (x_mi == -2 && x_ma == 3 && y_mi == -2 && y_ma == 3) {
-        // interior: the same loop fully unrolled (weights become immediates)
+        // interior, in fixed point: the weights are 6/16, 4/16, 1/16, so every
+        // term is val * W / 256 (W integer <= 36) and every partial sum of the
+        // reference's float loop is an exact float (numerator < 65536 * 256 =
+        // 2^24); the integer sums scaled by 2^-8 are those same floats
+        int isum = 0, iwall = 0;
 #pragma unroll
         for (int yi = -2; yi < 3; ++yi) {
             const uint16_t *r = t[2 * y + yi - oy] - ox;
 #pragma unroll
             for (int xi = -2; xi < 3; ++xi) {
-                int val = r[2 * x + xi];
-                if (abs(val - center) < 90) {  // 3 * sigma_color = 90.0f exactly
-                    sum += val * weights[xi < 0 ? -xi : xi] * weights[yi < 0 ? -yi : yi];
-                    wall += weights[xi < 0 ? -xi : xi] * weights[yi < 0 ? -yi : yi];
-                }
+                const int val = r[2 * x + xi];
+                const int w = (xi == 0 ? 6 : (xi == 1 || xi == -1 ? 4 : 1)) * (yi == 0 ? 6 : (yi == 1 || yi == -1 ? 4 : 1));
+                const bool ok = abs(val - center) < 90;  // 3 * sigma_color = 90.0f exactly
+                isum += ok ? val * w : 0;
+                iwall += ok ? w : 0;
             }
         }
+        sum = (float)isum * 0.00390625f;
+        wall = (float)iwall * 0.00390625f;
     } else {
         for (int yi = y_mi; yi < y_ma; ++yi) {
             const uint16_t *r = t[2 * y + yi - oy] - ox;
@@ -367,10 +373,13 @@ __device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[
                 const float *r = dt[cy0 + i - oy] - ox + cx0;
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
-                    if (!isnan(r[j])) {
-                        sum += r[j] * (float)gauss_w(4 - i, 4 - j);
-                        count += gauss_w(4 - i, 4 - j);
-                    }
+                    // branch-free: a masked tap adds +0 (sum >= 0: depths); the
+                    // fused multiply-add is the contraction the compiler makes
+                    // of the reference's `sum += r * w`
+                    const float v = r[j];
+                    const bool ok = !isnan(v);
+                    sum = __fmaf_rn(ok ? v : 0.f, (float)gauss_w(4 - i, 4 - j), sum);
+                    count += ok ? gauss_w(4 - i, 4 - j) : 0;
                 }
             }
         } else {
@@ -390,17 +399,21 @@ __device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[
         float sum = 0;
         int count = 0;
         if (interior) {
+            // integer arithmetic: every partial sum of the reference's float
+            // loop is an integer below 2^24 (255 x 256), hence exact, so the
+            // integer sum converted to float is the same value
+            int isum = 0;
 #pragma unroll
             for (int i = 0; i < 5; ++i) {
                 const uint8_t *r = it[cy0 + i - oy] - ox + cx0;
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
-                    if (r[j] > 0) {
-                        sum += r[j] * (float)gauss_w(4 - i, 4 - j);
-                        count += gauss_w(4 - i, 4 - j);
-                    }
+                    const int v = r[j];
+                    isum += v * gauss_w(4 - i, 4 - j);
+                    count += v > 0 ? gauss_w(4 - i, 4 - j) : 0;
                 }
             }
+            sum = (float)isum;
         } else {
             for (int cy = cy0; cy < ty; ++cy) {
                 const uint8_t *r = it[cy - oy] - ox;
