@@ -5,11 +5,12 @@ Headline (value): warm-started batched tracking.  A step = one batch of
 --batch-pairs held-out 640x480 frame pairs (6x4x3 m rooms with 20 spheres,
 fx = fy = 525, depth noise 0.0012 z^2, 5 % dropout, relative motion <= 10 deg /
 10 cm) tracked by one odo_batch_track_warm call: the warm-start network's
-proposal for every pair, 3 pyramid levels with 3/2/2 ICP+RGB iterations and
+proposal for every pair, 3 pyramid levels with 2/2/2 ICP+RGB iterations and
 no SO3 stage, and a fall-back to the reference's schedule (SO3 + 10/5/4) for
 the pairs whose residual or proposal disagreement fails the test.  The
 network is trained first, on the GPU, by the library's own kernels, on
-GPU-rendered pairs labelled by the plain tracker (setup, not timed).  Two
+150,000 GPU-rendered pairs labelled by the plain tracker (setup, about 2.5
+minutes, not timed).  Two
 batches (> L2) are resident in HBM and alternate.  Beside it, on the same
 pairs: the plain batched tracker (odo_batch_track), and the plain
 single-pair drop-in path (one frame per call through the reference's call
@@ -81,12 +82,12 @@ def parse():
     ap.add_argument("--prefetch", action="store_true", help="enable the iteration kernels' L2 bulk prefetch")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
-    ap.add_argument("--train-pairs", type=int, default=100000, help="warm study: rendered training pairs")
-    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--train-pairs", type=int, default=150000, help="warm study: rendered training pairs")
+    ap.add_argument("--epochs", type=int, default=50)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-pairs", type=int, default=2000)
     ap.add_argument("--warm-levels", type=int, default=3)
-    ap.add_argument("--warm-iters", default="3,2,2")
+    ap.add_argument("--warm-iters", default="2,2,2")
     ap.add_argument("--max-disagree", type=float, default=5.0, help="warm study: fall-back angle (deg)")
     ap.add_argument("--oracle-pairs", type=int, default=24, help="warm study: pairs also tracked by the FP64 oracle")
     ap.add_argument("--save-params", default=None)

@@ -397,7 +397,7 @@ class WarmStartTracker:
     (`plain_residual`, the median over the training pairs) or when the refined
     pose differs from the proposal by more than `max_disagree_deg`."""
 
-    def __init__(self, net, batch, plain_residual, levels=3, iterations=(3, 2, 2), residual_ratio=6.0,
+    def __init__(self, net, batch, plain_residual, levels=3, iterations=(2, 2, 2), residual_ratio=6.0,
                  max_disagree_deg=5.0, max_pairs=512):
         import torch
         self.net, self.batch = net, batch
