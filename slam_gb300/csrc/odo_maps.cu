@@ -16,24 +16,29 @@ namespace {
 
 constexpr int BX = 32, BY = 8;
 
-// Linear enumeration of the 32 x kTileRows tiles of all pyramid levels
-// (level l is (cols >> l) x (rows >> l)), so that a multi-level launch has no
-// blocks for pixels outside a level; a 32x8 block covers a tile in
-// kTileRows / 8 passes.
-constexpr int kTileRows = 32;
+// Output rows per block of the per-pixel preprocessing kernels: 32 for
+// batches (a block's memory round trip shared by 1024 outputs), 8 for a
+// single frame (enough blocks to fill the GPU from one 640x480 image).
+constexpr int kTileRowsBatch = 32, kTileRowsSingle = 8;
+
+// Linear enumeration of the 32 x th tiles of all pyramid levels (level l is
+// (cols >> l) x (rows >> l)), so that a multi-level launch has no blocks for
+// pixels outside a level; a 32x8 block covers a tile in th / 8 passes.
 struct LevelTiles {
     int tx[kLevels];     // tiles per row of each level
     int start[kLevels];  // first linear tile of each level
     int total;
+    int th;              // tile rows
 };
-inline LevelTiles level_tiles(int cols, int rows, int nlevels) {
+inline LevelTiles level_tiles(int cols, int rows, int nlevels, int th) {
     LevelTiles t{};
+    t.th = th;
     int s = 0;
     for (int l = 0; l < kLevels; ++l) {
         const int c = l < nlevels ? cols >> l : 0, r = l < nlevels ? rows >> l : 0;
         t.tx[l] = (c + BX - 1) / BX;
         t.start[l] = s;
-        s += t.tx[l] * ((r + kTileRows - 1) / kTileRows);
+        s += t.tx[l] * ((r + th - 1) / th);
     }
     t.total = s;
     return t;
@@ -43,20 +48,23 @@ __device__ __forceinline__ void tile_origin(const LevelTiles &t, int b, int &l, 
     l = b >= t.start[2] ? 2 : (b >= t.start[1] ? 1 : 0);
     const int k = b - t.start[l];
     X0 = (k % t.tx[l]) * BX;
-    Y0 = (k / t.tx[l]) * kTileRows;
+    Y0 = (k / t.tx[l]) * t.th;
 }
 
-// The window kernels stage the source pixels of their 32x8 block in shared
+// The window kernels stage the source pixels of their block in shared
 // memory (coalesced loads, each source pixel read once) and then run the
-// reference's window loops unchanged on the tile.  A 2x downsampling 5x5
-// window of the block's 32 x 32 outputs covers source columns
-// [2 X0 - 2, 2 X0 + 65) and rows [2 Y0 - 2, 2 Y0 + 65); the same-level 3x3 /
-// 4x4 windows of the derivative kernel cover [X0 - 2, X0 + 33) x
-// [Y0 - 2, Y0 + 33).  Each thread computes four outputs (rows 8 apart), so a
-// block's load round trip is shared by 1024 outputs.  Tile entries outside
-// the image are never read (the loops clamp to the image).
-constexpr int kDownTW = 2 * BX + 4, kDownTH = 2 * kTileRows + 4;
-constexpr int kDerTW = BX + 4, kDerTH = kTileRows + 4;
+// reference's window loops unchanged on the tile.  A block of 32x8 threads
+// computes 32 x TR outputs (TR / 8 per thread, rows 8 apart).  A 2x
+// downsampling 5x5 window of those outputs covers source columns
+// [2 X0 - 2, 2 X0 + 65) and rows [2 Y0 - 2, 2 Y0 + 2 TR + 1); the same-level
+// 3x3 / 4x4 windows of the derivative kernel cover [X0 - 2, X0 + 33) x
+// [Y0 - 2, Y0 + TR + 1).  Tile entries outside the image are never read
+// (the loops clamp to the image).
+constexpr int kDownTW = 2 * BX + 4, kDerTW = BX + 4;
+template <int TR>
+__host__ __device__ constexpr int down_th() { return 2 * TR + 4; }
+template <int TR>
+__host__ __device__ constexpr int der_th() { return TR + 4; }
 // All loads of a thread are issued before the first store to shared memory
 // (a register array of compile-time size), so a block waits for one memory
 // round trip, not one per element.  Blocks are BX x BY threads.
@@ -81,7 +89,8 @@ __device__ __forceinline__ void load_tile(const Img<const T> &src, int ox, int o
 
 // pyrDownGaussKernel, src/odom/utils.cu:57-94 (sigma_color = 30, :103), on
 // a shared-memory tile of the source; (X0, Y0) = the block's first output.
-__device__ __forceinline__ void pyr_out(const PyrArgs &a, const uint16_t (&t)[kDownTH][kDownTW], int ox, int oy,
+template <int TR>
+__device__ __forceinline__ void pyr_out(const PyrArgs &a, const uint16_t (&t)[down_th<TR>()][kDownTW], int ox, int oy,
                                         int x, int y) {
     const Img<const uint16_t> src = a.src;
     const Img<uint16_t> dst = a.dst;
@@ -129,16 +138,21 @@ __device__ __forceinline__ void pyr_out(const PyrArgs &a, const uint16_t (&t)[kD
     }
     at(dst, x, y) = static_cast<int>(sum / wall);
 }
+template <int TR>
 __device__ __forceinline__ void pyr_tile(const PyrArgs &a, int X0, int Y0) {
-    __shared__ uint16_t t[kDownTH][kDownTW];
+    __shared__ uint16_t t[down_th<TR>()][kDownTW];
     const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
     load_tile(a.src, ox, oy, t);
     __syncthreads();
 #pragma unroll 1
-    for (int r = 0; r < kTileRows / BY; ++r) pyr_out(a, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+    for (int r = 0; r < TR / BY; ++r) pyr_out<TR>(a, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
-__global__ void k_pyr_down_depth(PyrArgs a) { pyr_tile(a, blockIdx.x * BX, blockIdx.y * kTileRows); }
-__global__ void k_pyr_down_depth_b(const PyrArgs *A) { pyr_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRows); }
+__global__ void k_pyr_down_depth(PyrArgs a) {
+    pyr_tile<kTileRowsSingle>(a, blockIdx.x * BX, blockIdx.y * kTileRowsSingle);
+}
+__global__ void k_pyr_down_depth_b(const PyrArgs *A) {
+    pyr_tile<kTileRowsBatch>(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
+}
 
 // computeVmapKernel, src/odom/utils.cu:109-133, for one pixel.
 __device__ __forceinline__ float3 vertex_at(const Img<const uint16_t> &depth, int u, int v, float fx_inv,
@@ -180,7 +194,7 @@ __device__ __forceinline__ void vnmap_tile(const VNArgs &a, const LevelTiles &t)
     int l, X0, Y0;
     tile_origin(t, blockIdx.x, l, X0, Y0);
 #pragma unroll 1
-    for (int r = 0; r < kTileRows / BY; ++r) vnmap_px(a, l, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+    for (int r = 0; r < t.th / BY; ++r) vnmap_px(a, l, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
 __global__ void k_vmap_nmap(VNArgs a, LevelTiles t) { vnmap_tile(a, t); }
 __global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) { vnmap_tile(A[blockIdx.z], t); }
@@ -351,8 +365,9 @@ __host__ __device__ constexpr int gauss_w(int i, int j) {
 // pyrDownKernelIntensityGauss (src/odom/utils.cu:470-500) in one launch:
 // masked 5x5 Gaussian, window clamped at cols-1/rows-1 (exclusive), reversed
 // kernel index, int count.
-__device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[kDownTH][kDownTW],
-                                          const uint8_t (&it)[kDownTH][kDownTW], int ox, int oy, int x, int y) {
+template <int TR>
+__device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[down_th<TR>()][kDownTW],
+                                          const uint8_t (&it)[down_th<TR>()][kDownTW], int ox, int oy, int x, int y) {
     const Img<float> ddst = a.ddst;
     const Img<const uint8_t> isrc = a.isrc;
     const Img<uint8_t> idst = a.idst;
@@ -428,18 +443,23 @@ __device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[
         at(idst, x, y) = (sum / (float)count);
     }
 }
+template <int TR>
 __device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
-    __shared__ float dt[kDownTH][kDownTW];
-    __shared__ uint8_t it[kDownTH][kDownTW];
+    __shared__ float dt[down_th<TR>()][kDownTW];
+    __shared__ uint8_t it[down_th<TR>()][kDownTW];
     const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
     if (a.do_depth) load_tile(a.dsrc, ox, oy, dt);
     load_tile(a.isrc, ox, oy, it);
     __syncthreads();
 #pragma unroll 1
-    for (int r = 0; r < kTileRows / BY; ++r) gauss_out(a, dt, it, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+    for (int r = 0; r < TR / BY; ++r) gauss_out<TR>(a, dt, it, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
-__global__ void k_gauss_down(GaussArgs a) { gauss_tile(a, blockIdx.x * BX, blockIdx.y * kTileRows); }
-__global__ void k_gauss_down_b(const GaussArgs *A) { gauss_tile(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRows); }
+__global__ void k_gauss_down(GaussArgs a) {
+    gauss_tile<kTileRowsSingle>(a, blockIdx.x * BX, blockIdx.y * kTileRowsSingle);
+}
+__global__ void k_gauss_down_b(const GaussArgs *A) {
+    gauss_tile<kTileRowsBatch>(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
+}
 
 __constant__ float c_sobel_x[9] = {0.52201f, 0.00000f, -0.52201f, 0.79451f, -0.00000f,
                                    -0.79451f, 0.52201f, 0.00000f, -0.52201f};
@@ -452,7 +472,8 @@ __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.000
 // src/odom/reduce.cu:782-810: j0 < cols-5, i < rows-1, no zero intensity in
 // the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
 // into a byte mask, so the per-iteration pass reads one byte per pixel.
-__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_t (&t)[kDerTH][kDerTW], int ox,
+template <int TR>
+__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_t (&t)[der_th<TR>()][kDerTW], int ox,
                                          int oy, int x, int y) {
     const Img<const uint8_t> src = a.src[l];
     if (x >= src.cols || y >= src.rows) return;
@@ -506,29 +527,28 @@ __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_
     }
     at(a.cand[l], x, y) = c ? 1 : 0;
 }
+template <int TR>
 __device__ __forceinline__ void deriv_tile(const DerivArgs &a, const LevelTiles &lt) {
-    __shared__ uint8_t t[kDerTH][kDerTW];
+    __shared__ uint8_t t[der_th<TR>()][kDerTW];
     int l, X0, Y0;
     tile_origin(lt, blockIdx.x, l, X0, Y0);
     const int ox = X0 - 2, oy = Y0 - 2;
     load_tile(a.src[l], ox, oy, t);
     __syncthreads();
 #pragma unroll 1
-    for (int r = 0; r < kTileRows / BY; ++r) deriv_px(a, l, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+    for (int r = 0; r < TR / BY; ++r) deriv_px<TR>(a, l, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
-__global__ void k_derivatives(DerivArgs a, LevelTiles t) { deriv_tile(a, t); }
-__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) { deriv_tile(A[blockIdx.z], t); }
+__global__ void k_derivatives(DerivArgs a, LevelTiles t) { deriv_tile<kTileRowsSingle>(a, t); }
+__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) { deriv_tile<kTileRowsBatch>(A[blockIdx.z], t); }
 
 inline dim3 grid2(int cols, int rows, int z = 1) { return dim3((cols + BX - 1) / BX, (rows + BY - 1) / BY, z); }
-// grid of the window kernels: 32 x kTileRows outputs per block
-inline dim3 grid_tall(int cols, int rows, int z = 1) {
-    return dim3((cols + BX - 1) / BX, (rows + kTileRows - 1) / kTileRows, z);
-}
+// grid of the window kernels: 32 x th outputs per block
+inline dim3 grid_tall(int cols, int rows, int z, int th) { return dim3((cols + BX - 1) / BX, (rows + th - 1) / th, z); }
 
 }  // namespace
 
 cudaError_t launch_pyr_down_depth(Img<const uint16_t> src, Img<uint16_t> dst, cudaStream_t s) {
-    k_pyr_down_depth<<<grid_tall(dst.cols, dst.rows), dim3(BX, BY), 0, s>>>(PyrArgs{src, dst});
+    k_pyr_down_depth<<<grid_tall(dst.cols, dst.rows, 1, kTileRowsSingle), dim3(BX, BY), 0, s>>>(PyrArgs{src, dst});
     return cudaGetLastError();
 }
 
@@ -545,7 +565,7 @@ cudaError_t launch_vmap_nmap(const Img<const uint16_t> *depth, const Map3 *vmap,
         a.cy[l] = K[l].cy;
     }
     a.cutoff = cutoff;
-    const LevelTiles t = level_tiles(depth[0].cols, depth[0].rows, nlevels);
+    const LevelTiles t = level_tiles(depth[0].cols, depth[0].rows, nlevels, kTileRowsSingle);
     k_vmap_nmap<<<t.total, dim3(BX, BY), 0, s>>>(a, t);
     return cudaGetLastError();
 }
@@ -582,7 +602,7 @@ cudaError_t launch_rgbd_level0(const float *vz, size_t vz_pitch, const uint8_t *
 
 cudaError_t launch_gauss_down(Img<const float> dsrc, Img<float> ddst, Img<const uint8_t> isrc, Img<uint8_t> idst,
                               int do_depth, cudaStream_t s) {
-    k_gauss_down<<<grid_tall(idst.cols, idst.rows), dim3(BX, BY), 0, s>>>(GaussArgs{dsrc, ddst, isrc, idst, do_depth});
+    k_gauss_down<<<grid_tall(idst.cols, idst.rows, 1, kTileRowsSingle), dim3(BX, BY), 0, s>>>(GaussArgs{dsrc, ddst, isrc, idst, do_depth});
     return cudaGetLastError();
 }
 
@@ -598,17 +618,17 @@ cudaError_t launch_derivatives(const Img<const uint8_t> *src, const Img<int16_t>
         a.cand[l] = cand[l];
         a.minScale[l] = minScale[l];
     }
-    const LevelTiles t = level_tiles(src[0].cols, src[0].rows, nlevels);
+    const LevelTiles t = level_tiles(src[0].cols, src[0].rows, nlevels, kTileRowsSingle);
     k_derivatives<<<t.total, dim3(BX, BY), 0, s>>>(a, t);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pyr_down_depth_batch(const PyrArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_pyr_down_depth_b<<<grid_tall(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    k_pyr_down_depth_b<<<grid_tall(max_cols, max_rows, npairs, kTileRowsBatch), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_vmap_nmap_batch(const VNArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    const LevelTiles t = level_tiles(max_cols, max_rows, kLevels);
+    const LevelTiles t = level_tiles(max_cols, max_rows, kLevels, kTileRowsBatch);
     k_vmap_nmap_b<<<dim3(t.total, 1, npairs), dim3(BX, BY), 0, s>>>(args, t);
     return cudaGetLastError();
 }
@@ -622,11 +642,11 @@ cudaError_t launch_rgbd_level0_batch(const RgbdArgs *args, int npairs, int max_c
     return cudaGetLastError();
 }
 cudaError_t launch_gauss_down_batch(const GaussArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_gauss_down_b<<<grid_tall(max_cols, max_rows, npairs), dim3(BX, BY), 0, s>>>(args);
+    k_gauss_down_b<<<grid_tall(max_cols, max_rows, npairs, kTileRowsBatch), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_derivatives_batch(const DerivArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    const LevelTiles t = level_tiles(max_cols, max_rows, kLevels);
+    const LevelTiles t = level_tiles(max_cols, max_rows, kLevels, kTileRowsBatch);
     k_derivatives_b<<<dim3(t.total, 1, npairs), dim3(BX, BY), 0, s>>>(args, t);
     return cudaGetLastError();
 }
