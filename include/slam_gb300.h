@@ -194,8 +194,8 @@ int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOn
  * counterpart in the reference; used by the learned warm start). */
 int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init_dev, int rgbOnly,
                          float icpWeight, int fastOdom, odo_pair_result *results);
-/* Times every launch shape ({128, 256} threads x {2, 4, 8, 16, 32} pixels per
- * thread) on these pairs, keeps the fastest and returns it. */
+/* Times every launch shape ({128, 256} threads x {2, 4, 8, 16, 32, 64} pixels
+ * per thread) on these pairs, keeps the fastest and returns it. */
 int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
                        int so3, odo_pair_result *scratch_results, int *threads, int *pixels_per_thread,
                        float *best_ms);

@@ -706,14 +706,14 @@ int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rg
                        float *best_ms) {
     if (!b || !threads || !pixels_per_thread) return ODO_ERR_ARG;
     const int cand_t[2] = {128, 256};
-    const int cand_p[5] = {2, 4, 8, 16, 32};
+    const int cand_p[6] = {2, 4, 8, 16, 32, 64};
     float best = 1e30f;
     int bt = b->threads, bp = b->ppt;
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
     for (int ti = 0; ti < 2; ++ti)
-        for (int pi = 0; pi < 5; ++pi) {
+        for (int pi = 0; pi < 6; ++pi) {
             int rc = odo_batch_set_launch(b, cand_t[ti], cand_p[pi]);
             if (rc == ODO_OK) rc = odo_batch_track(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3, scratch_results);
             if (rc != ODO_OK) {

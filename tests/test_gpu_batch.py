@@ -70,7 +70,7 @@ def test_batch_autotune_runs(gpu):
     pairs = make_pairs(4, seed=3)
     b = BatchOdometry(4)
     t, ppt, ms = b.autotune(to_batch(pairs))
-    assert t in (128, 256) and ppt in (2, 4, 8, 16, 32) and ms > 0
+    assert t in (128, 256) and ppt in (2, 4, 8, 16, 32, 64) and ms > 0
 
 
 @pytest.mark.parametrize("launch", [(256, 2), (128, 32)], ids=["256x2", "128x32"])
