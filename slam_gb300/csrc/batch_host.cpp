@@ -386,24 +386,29 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
     }
 }
 
-cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, const int max_iters[kLevels]) {
+// prep = false skips the per-frame preprocessing whose results are already in
+// the pairs' buffers (a fall-back call right after the warm-started call on
+// the same slots) except the extra intensity pyramid the SO3 stage reads.
+cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, const int max_iters[kLevels],
+                          bool prep = true) {
     cudaStream_t s = b->stream;
     cudaError_t e = cudaMemcpyAsync(b->args_dev, b->args_host, b->args_bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
     auto A = [&](size_t o) { return (const void *)(b->args_dev + o); };
     const int W = b->max_w, Hh = b->max_h;
     if (e == cudaSuccess) e = launch_stamp_batch(b->st_dev, n, s);
-    if (e == cudaSuccess) e = launch_model_maps_batch((const ModelArgs *)A(b->o_model), n, W, Hh, s);
-    const int roles = so3 ? 3 : 2;
-    for (int r = 0; r < roles && e == cudaSuccess; ++r)
+    if (e == cudaSuccess && prep) e = launch_model_maps_batch((const ModelArgs *)A(b->o_model), n, W, Hh, s);
+    const int roles = so3 ? 3 : 2, r0 = prep ? 0 : 2;
+    for (int r = r0; r < roles && e == cudaSuccess; ++r)
         e = launch_rgbd_level0_batch((const RgbdArgs *)A(b->o_rgbd[r]), n, W, Hh, s);
     for (int l = 0; l < 2 && e == cudaSuccess; ++l)
-        for (int r = 0; r < roles && e == cudaSuccess; ++r)
+        for (int r = r0; r < roles && e == cudaSuccess; ++r)
             e = launch_gauss_down_batch((const GaussArgs *)A(b->o_gauss[r][l]), n, W >> (l + 1), Hh >> (l + 1), s);
-    for (int l = 0; l < 2 && e == cudaSuccess; ++l)
+    for (int l = 0; l < 2 && e == cudaSuccess && prep; ++l)
         e = launch_pyr_down_depth_batch((const PyrArgs *)A(b->o_pyr[l]), n, W >> (l + 1), Hh >> (l + 1), s);
-    if (e == cudaSuccess) e = launch_vmap_nmap_batch((const VNArgs *)A(b->o_vn), n, W, Hh, s);
-    if (e == cudaSuccess && rgb) e = launch_derivatives_batch((const DerivArgs *)A(b->o_deriv), n, W, Hh, s);
+    if (e == cudaSuccess && prep) e = launch_vmap_nmap_batch((const VNArgs *)A(b->o_vn), n, W, Hh, s);
+    if (e == cudaSuccess && rgb && prep)
+        e = launch_derivatives_batch((const DerivArgs *)A(b->o_deriv), n, W, Hh, s);
     if (e == cudaSuccess && so3) e = launch_so3_batch((const So3Args *)A(b->o_so3), n, s);
     if (e == cudaSuccess) e = launch_track_begin_batch(b->st_dev, n, s);
     if (e == cudaSuccess && warm) e = launch_warm_seed_batch(b->st_dev, b->init_dev, n, s);
@@ -512,9 +517,12 @@ namespace {
 
 // graph = false enqueues the kernels directly (for one-off batch sizes, e.g.
 // the fall-back subset of a warm-started batch, where instantiating a graph
-// would cost more than it saves).
+// would cost more than it saves).  reuse_slots (graph-less calls only): the
+// arena slot of every pair, whose buffers already hold this frame pair's
+// preprocessing from the previous call; that preprocessing is skipped.
 int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init, int rgbOnly, float icpWeight,
-               int fastOdom, int so3, odo_pair_result *results, bool graph = true) {
+               int fastOdom, int so3, odo_pair_result *results, bool graph = true,
+               const int *reuse_slots = nullptr) {
     if (!b || !pairs || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
     for (int i = 0; i < npairs; ++i) {
         const odo_pair &q = pairs[i];
@@ -533,7 +541,14 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
         BCK(cudaEventRecord(b->order_ev, 0));
         BCK(cudaStreamWaitEvent(b->stream, b->order_ev, 0));
     }
-    int rc = ensure_layout(b, pairs, npairs);
+    bool reuse = reuse_slots != nullptr && !graph && b->arena != nullptr;
+    for (int i = 0; i < npairs && reuse; ++i) {
+        const int s = reuse_slots[i];
+        reuse = s >= 0 && s < (int)b->layout.size() && b->layout[s] == std::make_tuple(pairs[i].width, pairs[i].height);
+    }
+    int rc = ODO_OK;
+    if (reuse) b->slot.assign(reuse_slots, reuse_slots + npairs);
+    else rc = ensure_layout(b, pairs, npairs);
     if (rc != ODO_OK) return rc;
     const int rgb = rgbOnly || icpWeight < 100;
     build_args(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3);
@@ -547,7 +562,7 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
     if (warm && init != b->init_dev)
         BCK(cudaMemcpyAsync(b->init_dev, init, sizeof(float) * 6 * npairs, cudaMemcpyDeviceToDevice, b->stream));
     if (!graph) {
-        BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters));
+        BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters, !reuse));
     } else {
         GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt,
                  g_split_solve | (g_l2_prefetch << 1)};
@@ -629,6 +644,7 @@ int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, 
         for (int l = 0; l < kLevels; ++l) q.iterations[l] = wp->iterations[l];
     }
     rc = track_impl(b, warm.data(), npairs, b->init_dev, wp->rgbOnly, wp->icpWeight, wp->fastOdom, 0, results);
+    const std::vector<int> warm_slot = b->slot;  // where each pair's preprocessed buffers are
     const int rc2 = odo_cnn_wait(net);
     if (rc != ODO_OK) return rc;
     if (rc2 != ODO_OK) return rc2;
@@ -655,12 +671,20 @@ int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, 
         if (fb) idx.push_back(i);
     }
     if (idx.empty()) return ODO_OK;
-    // 4. the pairs that fell back: plain schedule with the SO3 stage
+    // 4. the pairs that fell back: plain schedule with the SO3 stage, on the
+    //    preprocessing of step 2 (same inputs, same slots) when it covered
+    //    every pyramid level these pairs use
     std::vector<odo_pair> sub;
-    for (int i : idx) sub.push_back(pairs[i]);
+    std::vector<int> sub_slot;
+    bool reuse = true;
+    for (int i : idx) {
+        sub.push_back(pairs[i]);
+        sub_slot.push_back(warm_slot[i]);
+        reuse = reuse && pairs[i].levels <= wp->levels;
+    }
     std::vector<odo_pair_result> sres(idx.size());
     rc = track_impl(b, sub.data(), (int)sub.size(), nullptr, wp->rgbOnly, wp->icpWeight, wp->fastOdom, 1, sres.data(),
-                    false);
+                    false, reuse ? sub_slot.data() : nullptr);
     if (rc != ODO_OK) return rc;
     for (size_t k = 0; k < idx.size(); ++k) results[idx[k]] = sres[k];
     return ODO_OK;

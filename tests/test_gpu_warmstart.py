@@ -60,3 +60,20 @@ def test_warm_batch_not_worse_than_plain(trained):
     ok = (e_plain[:, 0] < np.radians(2.0)) & (e_warm[:, 0] < np.radians(2.0))
     assert np.median(e_warm[ok, 0]) <= 1.5 * np.median(e_plain[ok, 0])
     assert 0.0 <= fb.mean() < 1.0
+
+
+def test_fallback_pairs_equal_plain_tracking(trained):
+    """Pairs that fall back are re-tracked with the plain schedule on the
+    warm call's preprocessed buffers: bit for bit what a plain batched call
+    on those pairs returns."""
+    from slam_gb300.batch import result_pose
+    b, net, ps, plain_res, _ = trained
+    fps = ps.frame_pairs()
+    res, fb = b.track_warm(net, fps, levels=3, iterations=(2, 2, 2), residual_limit=1.0 * plain_res,
+                           max_disagree_deg=5.0)
+    idx = np.nonzero(fb)[0]
+    assert 0 < len(idx) < len(fps)
+    plain = b.track([fps[i] for i in idx])
+    for k, i in enumerate(idx):
+        assert np.array_equal(result_pose(res[i]), result_pose(plain[k])), i
+        assert list(res[i].iterations) == list(plain[k].iterations)
