@@ -895,9 +895,9 @@ def run_warm_study(args):
             if args.sweep:
                 rp0 = b.track(fps, descs=descs)
                 Pp0 = _res_array(rp0)[0]
-                for lv, it_ in ((3, (2, 2, 2)), (3, (3, 2, 2)), (3, (3, 3, 3)), (3, (4, 3, 3)), (2, (3, 3, 0)),
-                                (2, (4, 3, 0))):
-                    for ratio in (2.5, 4.0, 6.0):
+                for lv, it_ in ((3, (1, 2, 2)), (3, (2, 1, 1)), (3, (2, 2, 1)), (3, (2, 2, 2)), (3, (3, 2, 2)),
+                                (2, (2, 2, 0))):
+                    for ratio in (4.0, 6.0, 8.0):
                         kw = dict(wkw, levels=lv, iterations=it_, residual_limit=ratio * plain_res)
                         b.track_warm(net, fps, descs=descs, **kw)
                         torch.cuda.synchronize()
