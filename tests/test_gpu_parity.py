@@ -376,3 +376,14 @@ def test_errors_are_returned_not_fatal(gpu):
     assert e.value.status == 1
     with pytest.raises(TypeError):
         g.initRGB(torch.zeros((48, 64, 4), dtype=torch.float32, device="cuda"))
+
+
+def test_smoke_entry(gpu):
+    """The build entry point's smoke check (160x120 pair, GPU vs oracle)."""
+    import importlib.util
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("graft_entry", os.path.join(root, "__graft_entry__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.smoke()
