@@ -6,8 +6,10 @@
 // (cited per kernel) so results are identical, but several reference
 // launches are fused into one: vertex+normal maps for all levels, the whole
 // model-map pyramid with its transform, and one launch per pyramid step for
-// depth and intensity together.  Memory-bound, 32x8 thread blocks, one thread
-// per output pixel.
+// depth and intensity together.  Blocks of 32x8 threads; the window kernels
+// stage their source tile in shared memory and compute 32 x 8 (one frame) or
+// 32 x 32 (batches) outputs per block; the model-map kernel imports one
+// 32x32 input tile per block for all three levels.
 #include "odo_device.cuh"
 
 namespace slamgb {
