@@ -47,25 +47,21 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ICP+RGB tracking frames/s @640x480: warm-started vs plain, equal pose error"
 BYTES_PER_PX_ITER = 62  # ICP 48 B (4 maps x 12 B) + photometric 14 B per pixel-iteration
-# the association/residual kernel's bytes: inputs 62 B (ICP maps 48 B +
-# nextImage 1 + nextDepth 4 + lastDepth 4 + lastImage 1 + dIdx/dIdy 4) and the
-# 16-byte correspondence record it writes for the photometric reduction
-# (which reads that record and nothing else)
-PASS1_BYTES_PER_PX = 62 + 16
-# DRAM bytes (read + write) per pixel of the association kernel from ncu
-# captures on GB300 (profiles/k_icp_rgbres_b_L0_48pairs_640x480.md: 826.9 MB
-# read + 223.8 MB written for 48 x 307,200 px;
-# profiles/k_icp_rgbres_L0_single_640x480.md: 17.1 MB for 307,200 px);
-# traffic grows with the pixels processed
-PASS1_TRAFFIC_PER_PX_BATCH = (826.9e6 + 223.8e6) / (48 * 307200)
-PASS1_TRAFFIC_PER_PX_SINGLE = 17.1e6 / 307200
+# the association kernel's algorithmic bytes are the 62 B of its inputs; the
+# correspondence record it writes for the photometric pass (an artefact of
+# the two-pass structure, as the reference's DataTerm is) is reported apart
+RECORD_BYTES_PER_PX = 16
+# one-kernel ncu captures of this build whose `dram_bytes_per_px:` lines give
+# the measured traffic per pixel (traffic grows with the pixels processed)
+TRAFFIC_PROFILE_BATCH = "k_icp_rgbres_b_L0_48pairs_640x480.md"
+TRAFFIC_PROFILE_SINGLE = "k_icp_rgbres_L0_single_640x480.md"
 PREPROC_BYTES_PER_PX = 140  # per-frame map/pyramid building, per level-0 pixel (x 4/3 over the pyramid)
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pool", type=int, default=64)
@@ -79,7 +75,6 @@ def parse():
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
     ap.add_argument("--launch", default=None, help="batch study: fixed launch shape THREADSxPIXELS (e.g. 128x8)")
-    ap.add_argument("--prefetch", action="store_true", help="enable the iteration kernels' L2 bulk prefetch")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
                     help="batch study: resolutions drawn uniformly from 160x120/320x240/640x480, or 640x480 only")
     ap.add_argument("--train-pairs", type=int, default=150000, help="warm study: rendered training pairs")
@@ -94,7 +89,8 @@ def parse():
     ap.add_argument("--load-params", default=None, help="warm study: skip training, use these parameters")
     ap.add_argument("--sweep", action="store_true", help="warm study: also evaluate other warm schedules")
     ap.add_argument("--batch-pairs", type=int, default=500, help="pairs per warm-started batched step")
-    ap.add_argument("--batch-steps", type=int, default=6, help="timed warm-started batched steps")
+    ap.add_argument("--verify-pairs", type=int, default=512,
+                    help="pairs per launch of the batched-verification line (0: skip it)")
     ap.add_argument("--residual-ratio", type=float, default=6.0)
     a = ap.parse_args()
     if a.pairs is None:
@@ -279,6 +275,7 @@ def run_ours(args):
     torch.cuda.synchronize()
 
     # ---- device-resident inputs -------------------------------------------
+    n_single = max(args.steps, 300)  # side measurement: a fixed sample of frames
     clocks = ClockSampler(local)
     clocks.start()
     if world > 1:
@@ -287,7 +284,7 @@ def run_ours(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     poses = []
     e0.record(stream)
-    for k in range(args.steps):
+    for k in range(n_single):
         poses.append(step(dframes[k % len(dframes)]))
     e1.record(stream)
     torch.cuda.synchronize()
@@ -297,7 +294,7 @@ def run_ours(args):
         tt = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         ms = float(tt.item())
-    fps = world * args.steps / (ms / 1000.0)
+    fps = world * n_single / (ms / 1000.0)
     errs = [synth.pose_error(synth.pose(np.float64(R), np.float64(t)), frames[k]["T2"])
             for k, (t, R) in enumerate(poses[:len(frames)])]
 
@@ -311,7 +308,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2.record(stream)
-    for k in range(args.steps):
+    for k in range(n_single):
         h = hframes[k % len(hframes)]
         for key in ekeys:
             stage[key].copy_(h[key], non_blocking=True)
@@ -323,7 +320,7 @@ def run_ours(args):
         tt = torch.tensor([ms_e2e], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         ms_e2e = float(tt.item())
-    fps_e2e = world * args.steps / (ms_e2e / 1000.0)
+    fps_e2e = world * n_single / (ms_e2e / 1000.0)
 
     # ---- roofline of the dominant kernel (association + residual pass) ----
     odo.profile(reset=True)
@@ -333,7 +330,7 @@ def run_ours(args):
     k_ms, s_ms, it_ms = odo.time_iteration(0, reps=100)
     level_ms["L0"] = [k_ms, s_ms, it_ms]
     n0 = cam.width * cam.height
-    alg_bytes = PASS1_BYTES_PER_PX * n0
+    alg_bytes = BYTES_PER_PX_ITER * n0
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     launches_per_frame = 10 + 4 + 2 * (10 + 5 + 4)
@@ -354,7 +351,7 @@ def run_ours(args):
             cpu = {"value": None, "unit": "frames/s", "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
         rot = [e[0] for e in errs]
         tr = [e[1] for e in errs]
-        plain = {"frames_per_s": fps, "ms_per_frame": ms / args.steps, "steps": args.steps,
+        plain = {"frames_per_s": fps, "ms_per_frame": ms / n_single, "steps": n_single,
                  "workload": "640x480 frame-to-model tracking, one frame per call (the drop-in path), synthetic "
                              f"300-frame room trajectory, first {len(frames)} frames cycled",
                  "levels": ["640x480", "320x240", "160x120"], "iterations": [10, 5, 4], "icpWeight": 10,
@@ -365,36 +362,41 @@ def run_ours(args):
                          "d2h_bytes_per_step": int(_native.load().odo_state_bytes())},
                  "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres (level 0)", "achieved": achieved,
                               "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                              "traffic": PASS1_TRAFFIC_PER_PX_SINGLE * n0, "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
+                              "traffic": (profile_traffic(TRAFFIC_PROFILE_SINGLE) or 0) * n0 or None,
+                              "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
                               "alg_bytes_per_launch": alg_bytes,
                               "note": "level-0 maps (~20 MB) are L2-resident within a frame"},
                  "frame_bytes": frame_bytes(cam, iters[1:]),
-                 "frame_roofline_gbs": frame_bytes(cam, iters[1:]) / (ms / args.steps * 1e-3) / 1e9,
+                 "frame_roofline_gbs": frame_bytes(cam, iters[1:]) / (ms / n_single * 1e-3) / 1e9,
                  "pose_error_vs_gt": {"rot_rad_mean": float(np.mean(rot)), "trans_m_mean": float(np.mean(tr)),
                                       "rot_rad_max": float(np.max(rot)), "trans_m_max": float(np.max(tr))},
                  "iterations": iters, "clocks": clk, "iteration_ms_by_level": level_ms,
-                 "device_phases_us": phases, "gpu_launches": launches_per_frame * args.steps}
+                 "device_phases_us": phases, "gpu_launches": launches_per_frame * n_single}
     warm = measure_warm_batched(args, stream, local, world)
+    verif = measure_batched_verification(args, stream, world) if args.verify_pairs > 0 else None
     if rank == 0:
         W = warm
         out = {"metric": METRIC, "value": W["fps"], "unit": "frames/s", "n_gpus": world, "steps": W["steps"],
                "warmup": W["warmup"], "ms_per_step": W["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": {"workload": f"warm-started batched tracking: {W['batch_pairs']} held-out 640x480 room pairs "
-                                      "per step (6x4x3 m rooms, 20 spheres, motion <= 10 deg / 10 cm), network "
-                                      f"proposal + {args.warm_levels} levels {args.warm_iters} without SO3, fall-back "
-                                      "to the plain schedule",
-                          "batch_pairs": W["batch_pairs"], "warm_schedule": W["schedule"],
-                          "fallback": W["fallback_cfg"], "train": W["train"], "launch": W["launch"],
+                                      f"per step, {W['eval_pairs']} held-out pairs cycled (6x4x3 m rooms, "
+                                      "20 spheres, motion <= 10 deg / 10 cm), network proposal + "
+                                      f"{args.warm_levels} levels {args.warm_iters} without SO3, fall-back to the "
+                                      "plain schedule",
+                          "batch_pairs": W["batch_pairs"], "eval_pairs": W["eval_pairs"],
+                          "warm_schedule": W["schedule"], "fallback": W["fallback_cfg"], "train": W["train"],
+                          "launch": W["launch"],
                           "l2": f"inputs larger than L2: {W['pool_batches']} batches x {W['batch_bytes'] / 1e9:.1f} GB "
-                                "resident in HBM, alternating",
+                                "resident in HBM, cycled",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
                "e2e": W["e2e"], "roofline": W["roofline"],
                "plain_batched": W["plain_batched"], "plain_single_pair": plain,
                "speedup": {"vs_plain_single_pair": W["fps"] / plain["frames_per_s"],
-                           "vs_plain_batched": W["fps"] / W["plain_batched"]["frames_per_s"]},
-               "pose_error_vs_gt": W["pose_error_vs_gt"], "fallback_rate": W["fallback_rate"],
-               "iterations_mean": W["iterations_mean"], "clocks": W["clocks"],
+                           "vs_plain_batched": W["fps"] / W["plain_batched"]["frames_per_s"],
+                           "eval_thresholds_vs_plain_batched": W["eval_thresholds"]["speedup_vs_plain_batched"]},
+               "eval_thresholds": W["eval_thresholds"], "accuracy": W["accuracy"],
+               "batched_verification": verif, "clocks": W["clocks"],
                "gpu_launches": W["gpu_launches"], "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -402,13 +404,68 @@ def run_ours(args):
     return out
 
 
+def profile_traffic(name):
+    """DRAM bytes (read + write) per pixel of a kernel, from the
+    `dram_bytes_per_px:` line of the committed ncu summary profiles/<name>
+    (a one-kernel capture of this build); None when absent."""
+    import re
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                m = re.match(r"\s*[-*]?\s*`?dram_bytes_per_px:\s*([0-9.]+)", line)
+                if m:
+                    return float(m.group(1))
+    except OSError:
+        pass
+    return None
+
+
+def oracle_distance(pool, res_sets, npairs):
+    """FP64 oracle (plain schedule, the reference's call order) on the first
+    `npairs` pairs of pool[0]: the distance of each result set's poses from
+    it.  res_sets: {name: results of pool[0]}."""
+    import torch
+    from oracle import oracle
+    from slam_gb300 import DEFAULT_ANGLE_THRESH, DEFAULT_DIST_THRESH, synth
+    from slam_gb300.batch import result_pose
+    ps = pool[0]
+    cam = ps.cam
+    oracle.set_threads(os.cpu_count() or 1)
+    d = {k: [] for k in res_sets}
+    for i in range(min(npairs, ps.n)):
+        h = {k: getattr(ps, k)[i].cpu().numpy() for k in ("model_vert", "model_norm", "model_rgba", "rgba")}
+        depth = ps.depth[i].cpu().view(torch.int16).numpy().view(np.uint16)
+        o = oracle.Odometry(cam.width, cam.height, cam.cx, cam.cy, cam.fx, cam.fy, DEFAULT_DIST_THRESH,
+                            DEFAULT_ANGLE_THRESH, prec=64)
+        T1 = ps.T1[i].astype(np.float32)
+        o.initFirstRGB(h["model_rgba"])
+        o.initICPModel(h["model_vert"], h["model_norm"], 20.0, T1)
+        o.initRGBModel(h["model_rgba"])
+        o.initICP(depth, 20.0)
+        o.initRGB(h["rgba"])
+        t, R = o.getIncrementalTransformation(T1[:3, 3], T1[:3, :3], False, 10.0, True, False, True)
+        o.close()
+        T64 = synth.pose(np.asarray(R, np.float64), np.asarray(t, np.float64))
+        for k, res in res_sets.items():
+            d[k].append(synth.pose_error(result_pose(res[i]), T64))
+    out = {"pairs": min(npairs, ps.n), "reference": "FP64 oracle, plain schedule (SO3 + 10/5/4)"}
+    for k, v in d.items():
+        v = np.array(v)
+        out[k] = {"within_1e-5": float(np.mean((v[:, 0] <= 1e-5) & (v[:, 1] <= 1e-5))),
+                  "rot_rad_p50": float(np.median(v[:, 0])), "trans_m_p50": float(np.median(v[:, 1])),
+                  "rot_rad_max": float(v[:, 0].max()), "trans_m_max": float(v[:, 1].max())}
+    return out
+
+
 def measure_warm_batched(args, stream, local, world):
     """The headline: warm-started batched tracking of 640x480 pairs (the
-    network trained here first, on the GPU, by the library's own kernels),
-    with the plain batched tracker timed on the same pairs."""
+    network trained here first, on the GPU, by the library's own kernels) over
+    the held-out evaluation set, with the plain batched tracker timed on the
+    same pairs and the evaluation's fall-back thresholds reported beside the
+    tuned ones."""
     import torch
     from slam_gb300 import synth, warmstart as ws
-    from slam_gb300.batch import BatchOdometry
+    from slam_gb300.batch import BatchOdometry, result_pose
     cam = synth.Camera()
     nb = args.batch_pairs
     b = BatchOdometry(nb, stream=stream.cuda_stream)
@@ -425,69 +482,102 @@ def measure_warm_batched(args, stream, local, world):
     n_train = int(ts["labels"].shape[0])
     del ts
     its = tuple(int(v) for v in args.warm_iters.split(","))
-    wkw = dict(levels=args.warm_levels, iterations=its, residual_limit=args.residual_ratio * plain_res,
-               max_disagree_deg=args.max_disagree)
-    pool = [ws.make_room_pairs(args.seed * 31 + 1000 + k, nb, cam, 10.0, 0.10) for k in range(2)]
+    tuned = dict(levels=args.warm_levels, iterations=its, residual_limit=args.residual_ratio * plain_res,
+                 max_disagree_deg=args.max_disagree)
+    spec = dict(levels=args.warm_levels, iterations=its, residual_limit=1.5 * plain_res, max_disagree_deg=0.5)
+    # held-out evaluation set: eval_pairs pairs in batches of nb, all resident
+    nbatch = max(1, -(-args.eval_pairs // nb))
+    pool = [ws.make_room_pairs(args.seed * 31 + 1000 + k, nb, cam, 10.0, 0.10) for k in range(nbatch)]
     fps = [p.frame_pairs() for p in pool]
     descs = [b._descs(f) for f in fps]
     batch_bytes = sum(t[0].numel() * t[0].element_size() * nb for t in
                       (pool[0].model_vert, pool[0].model_norm, pool[0].model_rgba, pool[0].depth, pool[0].rgba))
     threads, ppt, _ = b.autotune(fps[0])
     W = max(args.warmup, 3)
-    K = args.batch_steps
+    K = args.steps
     for k in range(W):
-        b.track(fps[k % 2], descs=descs[k % 2])
-        b.track_warm(net, fps[k % 2], descs=descs[k % 2], **wkw)
-    # ---- warm-started, inputs resident in HBM ----
+        b.track(fps[k % nbatch], descs=descs[k % nbatch])
+        b.track_warm(net, fps[k % nbatch], descs=descs[k % nbatch], **tuned)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, steps):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(steps):
+            fn(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    # ---- warm-started, inputs resident in HBM: exactly K steps ----
     clocks = ClockSampler(local)
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    res_w, fb_all = [], []
-    e0.record(stream)
-    for k in range(K):
-        r, fb = b.track_warm(net, fps[k % 2], descs=descs[k % 2], **wkw)
-        res_w.append(r)
-        fb_all.append(fb)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_w = e0.elapsed_time(e1)
+    ms_w = timed(lambda k: b.track_warm(net, fps[k % nbatch], descs=descs[k % nbatch], **tuned), K)
     clk = clocks.stop()
     # ---- plain batched on the same pairs ----
-    torch.cuda.synchronize()
-    res_p = []
-    e0.record(stream)
-    for k in range(K):
-        res_p.append(b.track(fps[k % 2], descs=descs[k % 2]))
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_p = e0.elapsed_time(e1)
+    ms_p = timed(lambda k: b.track(fps[k % nbatch], descs=descs[k % nbatch]), K)
+    # ---- the evaluation's fall-back thresholds (residual > 1.5x plain, pose
+    # disagreement > 0.5 deg), one timed pass over the held-out set ----
+    spec_res = []
+    ms_s = timed(lambda k: spec_res.append(b.track_warm(net, fps[k], descs=descs[k], **spec)), nbatch)
     if world > 1:
-        tt = torch.tensor([ms_w, ms_p], device="cuda")
+        tt = torch.tensor([ms_w, ms_p, ms_s], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_w, ms_p = (float(v) for v in tt.tolist())
+        ms_w, ms_p, ms_s = (float(v) for v in tt.tolist())
+    # ---- accuracy over the whole held-out set (untimed) ----
+    tuned_res = [b.track_warm(net, fps[k], descs=descs[k], **tuned) for k in range(nbatch)]
+    plain_res_all = [list(b.track(fps[k], descs=descs[k])) for k in range(nbatch)]
+
+    def errs(res_list):
+        return np.array([synth.pose_error(result_pose(r), pool[k].T2[i])
+                         for k, res in enumerate(res_list) for i, r in enumerate(res)])
+
+    pct = lambda v: {"p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90))}
+    fail = lambda e: float(np.mean((e[:, 0] > np.radians(2.0)) | (e[:, 1] > 0.05)))
+    iters = lambda res_list: np.array([list(r.iterations) for res in res_list for r in res], np.float64)
+
+    def summary(res_list, fb_list=None):
+        e = errs(res_list)
+        out = {"rot_rad": pct(e[:, 0]), "trans_m": pct(e[:, 1]), "fail": fail(e),
+               "iterations_mean": iters(res_list).mean(axis=0).tolist()}
+        if fb_list is not None:
+            out["fallback_rate"] = float(np.mean(np.concatenate(fb_list)))
+        return out
+
+    acc_tuned = summary([r for r, _ in tuned_res], [f for _, f in tuned_res])
+    acc_spec = summary([r for r, _ in spec_res], [f for _, f in spec_res])
+    acc_plain = summary(plain_res_all)
+    it_plain = np.array(acc_plain["iterations_mean"])
+    saved = lambda a: float((it_plain[1:].sum() - np.array(a["iterations_mean"])[1:].sum()) / it_plain[1:].sum())
+    # distance from the FP64 oracle's plain tracking, on a sample of pairs
+    dist = oracle_distance(pool, {"warm_tuned": tuned_res[0][0], "warm_eval_thresholds": spec_res[0][0],
+                                  "plain_batched": plain_res_all[0]}, args.oracle_pairs)
     # ---- end to end: each step's inputs copied from pinned host memory ----
     # (double-buffered: step k+1's copies, split over N_COPY copy streams,
     # run while step k is tracked; the timed region holds every step's
     # copies and the read-back of its results)
+    # (two of the held-out batches in pinned host memory; step k copies
+    # batch k % 2 into its device buffer and tracks it)
     keys = ("model_vert", "model_norm", "model_rgba", "depth", "rgba")
-    host = [{k: getattr(p, k).cpu().pin_memory() for k in keys} for p in pool]
+    nh = min(2, nbatch)
+    host = [{k: getattr(pool[h], k).cpu().pin_memory() for k in keys} for h in range(nh)]
     N_COPY = 4
     css = [torch.cuda.Stream() for _ in range(N_COPY)]
     ev_copy = [[torch.cuda.Event() for _ in css] for _ in range(2)]
     ev_used = [torch.cuda.Event(), torch.cuda.Event()]
     chunk = -(-nb // N_COPY)
 
-    def issue_copy(buf, wait=True):
+    def issue_copy(k, wait=True):
+        buf = k % nh
         for j, c in enumerate(css):
             if wait:
                 c.wait_event(ev_used[buf])  # the step that last read this buffer is done
             with torch.cuda.stream(c):
                 for key in keys:
-                    getattr(pool[buf], key)[j * chunk:(j + 1) * chunk].copy_(
-                        host[buf][key][j * chunk:(j + 1) * chunk], non_blocking=True)
+                    getattr(pool[buf], key)[j * chunk:(j + 1) * chunk].copy_(host[buf][key][j * chunk:(j + 1) * chunk],
+                                                                               non_blocking=True)
             ev_copy[buf][j].record(c)
 
     # H2D bandwidth of one step's copies alone (after one untimed round)
@@ -507,11 +597,11 @@ def measure_warm_batched(args, stream, local, world):
     issue_copy(0)
     for k in range(K):
         if k + 1 < K:
-            issue_copy((k + 1) % 2)
-        for ev in ev_copy[k % 2]:
+            issue_copy(k + 1)
+        for ev in ev_copy[k % nh]:
             stream.wait_event(ev)
-        b.track_warm(net, fps[k % 2], descs=descs[k % 2], **wkw)
-        ev_used[k % 2].record(stream)
+        b.track_warm(net, fps[k % nh], descs=descs[k % nh], **tuned)
+        ev_used[k % nh].record(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1)
@@ -523,35 +613,28 @@ def measure_warm_batched(args, stream, local, world):
     b.track(fps[0], descs=descs[0])
     k_ms, s_ms, it_ms = b.time_iteration(0, reps=10)
     px = nb * cam.width * cam.height
-    alg = PASS1_BYTES_PER_PX * px
+    alg = BYTES_PER_PX_ITER * px
     peak, peak_kind = measured_peaks()
     achieved = alg / (k_ms * 1e-3) / 1e9
-    # ---- accuracy and iteration counts ----
-    def errs(res_list):
-        e = []
-        for k, res in enumerate(res_list):
-            T2 = pool[k % 2].T2
-            e += [synth.pose_error(np.array(r.pose, np.float64).reshape(4, 4), T2[i]) for i, r in enumerate(res)]
-        return np.array(e)
-    ew, ep = errs(res_w), errs(res_p)
-    pct = lambda v: {"p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90))}
-    fail = lambda e: float(np.mean((e[:, 0] > np.radians(2.0)) | (e[:, 1] > 0.05)))
-    it_w = np.array([list(r.iterations) for res in res_w for r in res], np.float64)
-    it_p = np.array([list(r.iterations) for res in res_p for r in res], np.float64)
-    fbr = float(np.mean(np.concatenate(fb_all)))
+    traffic_px = profile_traffic(TRAFFIC_PROFILE_BATCH)
     # kernels per warm step: packing + 8 GEMMs per 256 pairs, the warm graph
     # (stamp, model maps, 2 photometric inputs, 4 pyramid steps, 2 depth
     # pyramid steps, maps, derivatives, begin, seed, 3 per iteration, end) and
     # the fall-back batch with its SO3 stage
+    fbr = acc_tuned["fallback_rate"]
     gemm = -(-nb // 256) * 9
     warm_graph = 13 + 3 * sum(its[:args.warm_levels])
     plain_graph = 14 + 1 + 3 * 19
     launches = K * (gemm + warm_graph + (plain_graph if fbr > 0 else 0))
     return {"fps": K * nb / (ms_w * 1e-3), "ms_per_step": ms_w / K, "steps": K, "warmup": W, "batch_pairs": nb,
-            "pool_batches": 2, "batch_bytes": batch_bytes,
+            "eval_pairs": nbatch * nb, "pool_batches": nbatch, "batch_bytes": batch_bytes,
             "schedule": {"levels": args.warm_levels, "iterations": list(its), "so3": False},
-            "fallback_cfg": {"residual_limit": wkw["residual_limit"], "residual_ratio": args.residual_ratio,
+            "fallback_cfg": {"residual_limit": tuned["residual_limit"], "residual_ratio": args.residual_ratio,
                              "plain_residual_median": plain_res, "max_disagree_deg": args.max_disagree},
+            "eval_thresholds": {"residual_ratio": 1.5, "max_disagree_deg": 0.5,
+                                "frames_per_s": nbatch * nb / (ms_s * 1e-3), "ms_per_step": ms_s / nbatch,
+                                "speedup_vs_plain_batched": (nbatch * nb / (ms_s * 1e-3)) / (K * nb / (ms_p * 1e-3)),
+                                "iterations_saved": saved(acc_spec), **acc_spec},
             "train": {"pairs_rendered": args.train_pairs, "pairs_kept": n_train, "epochs": args.epochs,
                       "generation_s": gen_s, "train_s": train_s, "last_epoch_loss": hist[-1]},
             "launch": {"threads": threads, "pixels_per_thread": ppt},
@@ -560,21 +643,83 @@ def measure_warm_batched(args, stream, local, world):
                     "note": "copies of step k+1 (4 copy streams) overlap the tracking of step k (two input buffers)"},
             "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres_b (level 0, all pairs of a step)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": PASS1_TRAFFIC_PER_PX_BATCH * px,
-                         "traffic_source": "ncu capture of 48 pairs scaled to the launch's pixels",
-                         "kernel_ms": k_ms, "photometric_kernel_ms": s_ms,
-                         "iteration_ms": it_ms, "alg_bytes_per_launch": alg,
-                         "alg_bytes_per_px": PASS1_BYTES_PER_PX},
+                         "frac": achieved / peak, "alg_bytes_per_px": BYTES_PER_PX_ITER,
+                         "alg_bytes_per_launch": alg,
+                         "traffic": traffic_px * px if traffic_px else None,
+                         "traffic_source": "profiles/" + TRAFFIC_PROFILE_BATCH +
+                                           " (one-kernel ncu capture, DRAM bytes per pixel x the launch's pixels)",
+                         "record_bytes_per_px": RECORD_BYTES_PER_PX,
+                         "record_note": "the correspondence record the kernel writes for the photometric pass "
+                                        "is not algorithmic traffic; it is inside `traffic`",
+                         "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
+                         "iteration_frac": alg / (it_ms * 1e-3) / 1e9 / peak},
             "plain_batched": {"frames_per_s": K * nb / (ms_p * 1e-3), "ms_per_step": ms_p / K,
                               "schedule": "SO3 + 10/5/4, the reference's"},
-            "pose_error_vs_gt": {"warm": {"rot_rad": pct(ew[:, 0]), "trans_m": pct(ew[:, 1]), "fail": fail(ew)},
-                                 "plain_batched": {"rot_rad": pct(ep[:, 0]), "trans_m": pct(ep[:, 1]),
-                                                   "fail": fail(ep)},
-                                 "fail_definition": "error > 2 deg or > 5 cm"},
-            "fallback_rate": fbr,
-            "iterations_mean": {"warm": it_w.mean(axis=0).tolist(), "plain_batched": it_p.mean(axis=0).tolist(),
-                                "order": ["so3", "L0", "L1", "L2"]},
+            "accuracy": {"held_out_pairs": nbatch * nb, "warm_tuned": acc_tuned, "plain_batched": acc_plain,
+                         "iterations_saved_tuned": saved(acc_tuned),
+                         "fail_definition": "error > 2 deg or > 5 cm vs ground truth",
+                         "vs_fp64_oracle": dist},
             "clocks": clk, "gpu_launches": int(launches)}
+
+
+def measure_batched_verification(args, stream, world):
+    """Batched verification: args.verify_pairs pairs per launch at sizes drawn
+    uniformly from {160x120, 320x240, 640x480} (fx scaled), seeded rooms,
+    motion <= 8 deg / 15 cm, 2-3 pyramid levels, the reference's schedule with
+    SO3, one CUDA graph with the autotuned launch shape; pairs/s and the
+    per-pair device latency (p50 / p99)."""
+    import torch
+    from slam_gb300 import synth, warmstart as ws
+    from slam_gb300.batch import BatchOdometry, FramePair, result_pose
+    n = args.verify_pairs
+    rng = np.random.default_rng(args.seed * 7 + 5)
+    size_of = rng.integers(0, 3, size=n)
+    levels = rng.integers(2, 4, size=n)
+    sizes = [(160, 120), (320, 240), (640, 480)]
+    sets = {}
+    for si, (w, h) in enumerate(sizes):
+        cnt = int((size_of == si).sum())
+        if cnt:
+            sets[si] = ws.make_room_pairs(args.seed * 131 + si, cnt, synth.Camera().scaled(w, h), 8.0, 0.15)
+    fps, T2, next_of = [], [], {si: 0 for si in sets}
+    for i in range(n):
+        si = int(size_of[i])
+        ps, j = sets[si], next_of[si]
+        next_of[si] += 1
+        fps.append(FramePair(ps.cam, ps.model_vert[j], ps.model_norm[j], ps.model_rgba[j], ps.depth[j], ps.rgba[j],
+                             ps.model_rgba[j], ps.T1[j], levels=int(levels[i])))
+        T2.append(ps.T2[j])
+    b = BatchOdometry(n, stream=stream.cuda_stream)
+    threads, ppt, tune_ms = b.autotune(fps)
+    descs = b._descs(fps)
+    for _ in range(max(args.warmup, 3)):
+        b.track(fps, descs=descs)
+    K = max(args.steps, 3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(K):
+        res = b.track(fps, descs=descs)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    done = np.array([r.done_us for r in res])
+    err = np.array([synth.pose_error(result_pose(r), T) for r, T in zip(res, T2)])
+    return {"metric": "batched verification pairs/s", "value": n / (ms * 1e-3), "unit": "pairs/s",
+            "steps": K, "ms_per_step": ms,
+            "workload": f"{n} pairs per launch, sizes uniform over 160x120/320x240/640x480 "
+                        f"({', '.join('%dx%d: %d' % (sizes[k] + (int((size_of == k).sum()),)) for k in range(3))}), "
+                        "motion <= 8 deg / 15 cm, 2-3 levels, ICP+RGB with SO3, one CUDA graph",
+            "launch": {"threads": threads, "pixels_per_thread": ppt, "autotune_best_ms": tune_ms},
+            "latency_us": {"p50": float(np.percentile(done, 50)), "p99": float(np.percentile(done, 99)),
+                           "note": "device time from the batch's first kernel to the end of the pair's last solve; "
+                                   "all pairs advance level by level together"},
+            "pose_error_vs_gt": {"rot_rad_p50": float(np.median(err[:, 0])),
+                                 "trans_m_p50": float(np.median(err[:, 1]))}}
 
 
 def ctypes_sizeof_result():
@@ -1004,9 +1149,6 @@ def run_warm_study(args):
 
 def main():
     args = parse()
-    if args.prefetch:
-        from slam_gb300 import _native
-        _native.load().odo_debug_set_prefetch(1)
     if args.study == "warm":
         run_warm_study(args)
         return

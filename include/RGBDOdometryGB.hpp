@@ -23,8 +23,8 @@ class RGBDOdometryGB {
         Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
     };
 
-    RGBDOdometryGB(int width, int height, float cx, float cy, float fx, float fy, float distThresh = 0.10f,
-                   float angleThresh = 0.34202015f /* sin(20 deg) */) {
+    RGBDOdometryGB(int width, int height, float cx, float cy, float fx, float fy,
+                   float distThresh = ODO_DEFAULT_DIST_THRESH, float angleThresh = ODO_DEFAULT_ANGLE_THRESH) {
         check(odo_create(width, height, cx, cy, fx, fy, distThresh, angleThresh, &h_), "odo_create");
     }
     ~RGBDOdometryGB() { odo_destroy(h_); }

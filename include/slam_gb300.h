@@ -18,8 +18,9 @@
  * process (the reference's cudaSafeCall calls exit(0),
  * src/cuda/convenience.cuh:64-71).  A handle owns its device buffers and one
  * CUDA stream; it is not thread-safe, but separate handles are independent
- * (no globals, unlike the reference's __constant__/texture globals,
- * src/odom/utils.cu:548, 579-580).
+ * (no mutable globals, unlike the reference's __constant__/texture globals,
+ * src/odom/utils.cu:548, 579-580; the one exception is the fixed device
+ * array of the allocation-free entry point below, which needs no handle).
  *
  * Call order per frame, as in the reference (src/apps/elastic_fusion_file.cpp:367-374):
  *   odo_init_icp_model -> odo_init_rgb_model -> odo_init_icp_depth (or
@@ -48,6 +49,13 @@ extern "C" {
 
 typedef struct odo_handle odo_t;
 
+/* The reference's default thresholds (src/odom/RGBDOdometryef.h:35-36):
+ * distThresh = 0.10f, angleThresh = sin(20.f * 3.14159254f / 180.f), the
+ * latter evaluated as the reference evaluates it (float argument, result
+ * rounded to float). */
+#define ODO_DEFAULT_DIST_THRESH 0.10f
+#define ODO_DEFAULT_ANGLE_THRESH 0.342020094f
+
 /* The public metric members of RGBDOdometryef (src/odom/RGBDOdometryef.h:62-70). */
 typedef struct {
     float lastICPError;
@@ -61,8 +69,8 @@ typedef struct {
 } odo_stats;
 
 /* RGBDOdometryef::RGBDOdometryef, src/odom/RGBDOdometryef.cpp:21-111.
- * Pass distThresh = 0.10f and angleThresh = sinf(20 deg) for the reference
- * defaults (src/odom/RGBDOdometryef.h:35-36).  width/height must be >= 8 and
+ * Pass ODO_DEFAULT_DIST_THRESH and ODO_DEFAULT_ANGLE_THRESH for the
+ * reference defaults (src/odom/RGBDOdometryef.h:35-36).  width/height must be >= 8 and
  * <= 8192. */
 int odo_create(int width, int height, float cx, float cy, float fx, float fy, float distThresh, float angleThresh,
                odo_t **out);
@@ -152,7 +160,7 @@ typedef struct odo_batch odo_batch_t;
 typedef struct {
     int width, height;           /* level-0 size, 16..8192 */
     float fx, fy, cx, cy;
-    float distThresh, angleThresh; /* <= 0: reference defaults 0.10 m, sin(20 deg) */
+    float distThresh, angleThresh; /* <= 0: ODO_DEFAULT_DIST_THRESH, ODO_DEFAULT_ANGLE_THRESH */
     float depthCutoff;           /* <= 0: 20 m (maxDepthProcessed, src/configs/ef_file.cfg:16) */
     int levels;                  /* pyramid levels iterated, 1..3 */
     int iterations[3];           /* per-level Gauss-Newton iterations (0: the reference's 10 (3 fastOdom) / 5 / 4), <= 20 */
@@ -260,16 +268,19 @@ int odo_debug_derivatives(odo_t *h);
  * whole iteration.  Leaves the tracking state as it found it. */
 int odo_debug_time_iteration(odo_t *h, int level, int reps, float out_ms[3]);
 
-/* Process-wide switch of the L2 bulk prefetch of the next pixel chunk in the
- * iteration kernels (default 0: measured slower); takes effect for calls made
- * afterwards (a handle's captured graphs keep the value they were built with). */
-int odo_debug_set_prefetch(int on);
-
-/* Process-wide switch of the batched tracker's last iteration stage: 1
+/* The batched tracker's last iteration stage on this batch handle: 1
  * (default) the photometric pass and a one-block-per-pair solve kernel, 0 the
  * single-pair layout (the solve in the last block of the photometric pass).
  * Both give the same poses; takes effect for the next batch call. */
-int odo_batch_debug_set_split(int on);
+int odo_batch_debug_set_split(odo_batch_t *b, int on);
+
+/* Failure detection of the persistent mode's grid-wide barriers: each wait
+ * gives up after `polls` polls (default 2^26) and the tracking call returns
+ * ODO_ERR_TIMEOUT.  absent_block >= 0 makes that block of every persistent
+ * level kernel return at once without arriving at any barrier (a block that
+ * died), so that the others' waits run out; -1 (default) for normal work.
+ * The handle stays usable afterwards. */
+int odo_debug_set_wait_limit(odo_t *h, long long polls, int absent_block);
 
 /* Device-side phase timers accumulated over tracking calls (ns):
  * out[0] last-block reduction of the block partials, out[1] FP64 solve and
@@ -288,11 +299,10 @@ int odo_debug_history(odo_t *h, double *out, int max_rows);
  * cannot allocate device memory after start-up -- a tracker running inside
  * a fixed device-memory budget, or a real-time loop where cudaMalloc/cudaFree
  * would synchronise the device and stall other streams.  It computes one
- * ICP association + reduction pass like the reference's icpStep
- * (src/odom/reduce.cu:418-490): the caller passes the four planar maps
+ * ICP association + reduction pass: the caller passes the four planar maps
  * ([3][rows][cols] float, row pitch in bytes) and the poses; it returns the
  * 6x6 matrix A (row-major), b and {sum of squared residuals, inliers} on the
- * host, as icpStep does.  It needs no handle and allocates nothing: its
+ * host.  It needs no handle and allocates nothing: its
  * block partials live in one fixed device array of this library
  * (ODO_NOALLOC_SCRATCH_BYTES, held by every device that loads the library
  * until the process exits).
@@ -393,7 +403,10 @@ int odo_synth_render(const void *scenes_host, int nscenes, const int *view_scene
 /* C[M][N] (FP32) = A[M][K] B[N][K]^T with BF16 A, B (rows padded to a
  * multiple of 8 elements) on the tensor-core GEMM; bn = tile width 32..256,
  * layout = 0 (the library's operand layout), 1 (offsets exchanged; a
- * self-check of the layout) or 2 (layout 0 with FP16 operands). */
+ * self-check of the layout) or 2 (layout 0 with FP16 operands), plus 4 for
+ * the failure-detection test of the bounded tensor-core waits (one wait
+ * runs out on a barrier that nothing arrives at; returns ODO_ERR_TIMEOUT
+ * after draining the issued MMAs; needs K > 128). */
 int odo_cnn_debug_gemm(const uint16_t *A_dev, const uint16_t *B_dev, float *C_dev, int M, int N, int K, int bn,
                        int layout, void *stream);
 

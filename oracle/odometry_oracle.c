@@ -891,6 +891,14 @@ typedef struct {
     orc_stats st;
     double lastA[36], lastb[6];
     int so3_iters, iters_run[NUM_PYRS];
+    /* schedule override (levels > 0): the reference's per-level iteration
+     * counts (src/odom/RGBDOdometryef.cpp:382-384) restricted to the first
+     * `sched_levels` levels, each replaced by sched[l] where that is > 0 --
+     * how a batched pair with fewer pyramid levels or a short schedule runs */
+    int sched_levels, sched[NUM_PYRS];
+    /* keep_deriv != 0: the tracking call uses the derivative images already
+     * in dIdx/dIdy (set through odo_buffer) instead of computing them */
+    int keep_deriv;
     int nhist;
     double hist[32][9];
 } orc_odo;
@@ -1033,7 +1041,7 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
     const real maxDepthDeltaRGB = (real)0.07f;
     const float minGrad[3] = {5, 3, 1};
 
-    if (rgb)
+    if (rgb && !o->keep_deriv)
         for (int l = 0; l < NUM_PYRS; ++l)
             orc_derivatives(o->nextImage[l], o->dims_w[l], o->dims_h[l], o->dIdx[l], o->dIdy[l], NULL);
 
@@ -1103,6 +1111,9 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
     }
 
     int iterations[3] = {fastOdom ? 3 : 10, pyramid ? 5 : 0, pyramid ? 4 : 0};
+    if (o->sched_levels > 0)
+        for (int l = 0; l < NUM_PYRS; ++l)
+            iterations[l] = l < o->sched_levels ? (o->sched[l] > 0 ? o->sched[l] : iterations[l]) : 0;
     o->nhist = 0;
     real Rprev_inv[9];
     inv33_r(Rprev, Rprev_inv);
@@ -1237,6 +1248,15 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
     memcpy(o->st.lastA, o->lastA, sizeof(o->lastA));
     memcpy(o->st.lastb, o->lastb, sizeof(o->lastb));
 }
+
+/* Schedule override of the tracking loop (levels <= 0 restores the
+ * reference's schedule); iters may be NULL (the reference's counts). */
+void ORC(odo_set_schedule)(orc_odo *o, int levels, const int iters[3]) {
+    o->sched_levels = levels > NUM_PYRS ? NUM_PYRS : levels;
+    for (int l = 0; l < NUM_PYRS; ++l) o->sched[l] = iters ? iters[l] : 0;
+}
+
+void ORC(odo_set_keep_derivatives)(orc_odo *o, int keep) { o->keep_deriv = keep; }
 
 /* getCovariance, src/odom/RGBDOdometryef.cpp:597-600 */
 void ORC(odo_covariance)(orc_odo *o, double out[36]) { ORC(inverse6)(o->lastA, out); }

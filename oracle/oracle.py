@@ -298,6 +298,13 @@ class Odometry:
         self.k.f("odo_stats")(self._h, ctypes.byref(self._stats))
         return t, R.reshape(3, 3)
 
+    def set_schedule(self, levels, iterations=(0, 0, 0)):
+        """Iterate only the first `levels` pyramid levels, with iterations[l]
+        in place of the reference's count where it is > 0 (levels <= 0: the
+        reference's schedule) -- the batched tracker's per-pair schedule."""
+        it = (ctypes.c_int * 3)(*[int(v) for v in iterations])
+        self.k.f("odo_set_schedule")(self._h, int(levels), it)
+
     def getCovariance(self):
         out = np.zeros(36, np.float64)
         self.k.f("odo_covariance")(self._h, _p(out))
@@ -319,6 +326,19 @@ class Odometry:
         return {"lastICPError": s.lastICPError, "lastICPCount": s.lastICPCount, "lastRGBError": s.lastRGBError,
                 "lastRGBCount": s.lastRGBCount, "lastSO3Error": s.lastSO3Error, "lastSO3Count": s.lastSO3Count,
                 "lastA": np.array(s.lastA).reshape(6, 6), "lastb": np.array(s.lastb)}
+
+    def set_buffer(self, name, level, arr):
+        """Overwrites one of the handle's buffers (same shapes and types as
+        buffer())."""
+        cur = self.buffer(name, level)
+        a = np.ascontiguousarray(np.asarray(arr).astype(cur.dtype, copy=False).reshape(cur.shape))
+        ptr = self.k.f("odo_buffer")(self._h, self.BUF[name], level)
+        ctypes.memmove(ptr, a.ctypes.data, a.nbytes)
+
+    def keep_derivatives(self, keep=True):
+        """Tracking calls use the derivative images set with set_buffer
+        instead of computing them from nextImage."""
+        self.k.f("odo_set_keep_derivatives")(self._h, int(bool(keep)))
 
     def buffer(self, name, level):
         which = self.BUF[name]

@@ -112,9 +112,9 @@ SIGNATURES = [
     ("odo_debug_so3_step", c_int, [c_void_p, P(c_float), P(c_float), P(c_float), P(c_double)]),
     ("odo_debug_derivatives", c_int, [c_void_p]),
     ("odo_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
-    ("odo_debug_set_prefetch", c_int, [c_int]),
-    ("odo_batch_debug_set_split", c_int, [c_int]),
+    ("odo_batch_debug_set_split", c_int, [c_void_p, c_int]),
     ("odo_debug_profile", c_int, [c_void_p, P(c_double), c_int]),
+    ("odo_debug_set_wait_limit", c_int, [c_void_p, ctypes.c_longlong, c_int]),
     ("odo_debug_history", c_int, [c_void_p, P(c_double), c_int]),
     ("odo_cnn_param_count", c_size_t, []),
     ("odo_cnn_create", c_int, [c_int, P(c_void_p)]),

@@ -66,6 +66,11 @@ struct odo_batch {
     // offsets of the argument blocks in the argument arena
     size_t o_model, o_rgbd[3], o_gauss[3][2], o_pyr[2], o_vn, o_deriv, o_so3, o_pass[kLevels];
     int threads = 256, ppt = 2;
+    // 1: the last iteration stage is the photometric pass plus a
+    // one-block-per-pair solve kernel (the pass then carries no FP64 solve
+    // code and its registers); 0: the single-pair layout (the solve in the
+    // last block of the photometric pass).  Both give the same poses.
+    int split_solve = 1;
     int max_nb[kLevels];
     int max_w = 0, max_h = 0;
     float *init_dev = nullptr;  // [max_pairs][6] warm-start motions (odo_batch_track_init)
@@ -334,8 +339,8 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             L.nmap_curr = p.nc[l];
             L.vmap_prev = p.vp[l];
             L.nmap_prev = p.np[l];
-            L.angleThres = q.angleThresh > 0 ? q.angleThresh : 0.34202015f;
-            L.distThres = q.distThresh > 0 ? q.distThresh : 0.10f;
+            L.angleThres = q.angleThresh > 0 ? q.angleThresh : ODO_DEFAULT_ANGLE_THRESH;
+            L.distThres = q.distThresh > 0 ? q.distThresh : ODO_DEFAULT_DIST_THRESH;
             L.dIdx = Img<const int16_t>{p.dx[l].data, p.dx[l].pitch, p.dx[l].cols, p.dx[l].rows};
             L.dIdy = Img<const int16_t>{p.dy[l].data, p.dy[l].pitch, p.dy[l].cols, p.dy[l].rows};
             L.lastDepth = Img<const float>{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
@@ -347,7 +352,6 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             L.minScale = d.minScale[l];
             L.maxDepthDelta = 0.07f;
             L.sobelScale = sobelScale;
-            L.prefetch = g_l2_prefetch;  // the batch arena's own buffers
             a.st = b->st_dev + i;
             a.ws = p.ws;
             a.iters = (l < q.levels) ? (q.iterations[l] > 0 ? q.iterations[l] : base[l]) : 0;
@@ -415,7 +419,7 @@ cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, con
     for (int l = kLevels - 1; l >= 0 && e == cudaSuccess; --l)
         for (int j = 0; j < max_iters[l] && e == cudaSuccess; ++j)
             e = launch_level_iteration_batch((const PassArgs *)A(b->o_pass[l]), n, b->max_nb[l],
-                                             rgb ? b->max_nb[l] : 1, b->threads, 0, j, s);
+                                             rgb ? b->max_nb[l] : 1, b->threads, 0, j, s, 3, b->split_solve);
     if (e == cudaSuccess) e = launch_track_end_batch(b->st_dev, n, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_host, b->st_dev, sizeof(TrackState) * n, cudaMemcpyDeviceToHost, s);
     return e;
@@ -502,6 +506,13 @@ int odo_batch_set_stream(odo_batch_t *b, void *stream) {
     return ODO_OK;
 }
 
+int odo_batch_debug_set_split(odo_batch_t *b, int on) {
+    if (!b) return ODO_ERR_ARG;
+    if (b->split_solve != (on ? 1 : 0)) drop_graphs(b);
+    b->split_solve = on ? 1 : 0;
+    return ODO_OK;
+}
+
 int odo_batch_set_launch(odo_batch_t *b, int threads, int pixels_per_thread) {
     if (!b || (threads != 128 && threads != 256) || pixels_per_thread < 1 || pixels_per_thread > 64)
         return ODO_ERR_ARG;
@@ -565,7 +576,7 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
         BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters, !reuse));
     } else {
         GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt,
-                 g_split_solve | (g_l2_prefetch << 1)};
+                 b->split_solve};
         auto it = b->graphs.find(key);
         if (it == b->graphs.end()) {
             cudaGraph_t g = nullptr;
@@ -706,11 +717,11 @@ int odo_batch_debug_time_iteration(odo_batch_t *b, int level, int reps, float ou
         e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
             e = launch_level_iteration_batch(args, n, b->max_nb[level], b->last_rgb ? b->max_nb[level] : 1, b->threads,
-                                             0, 1, s, 3);
+                                             0, 1, s, 3, b->split_solve);
         if (e == cudaSuccess) e = cudaEventRecord(e0, s);
         for (int r = 0; r < reps && e == cudaSuccess; ++r)
             e = launch_level_iteration_batch(args, n, b->max_nb[level], b->last_rgb ? b->max_nb[level] : 1, b->threads,
-                                             0, 1, s, mask);
+                                             0, 1, s, mask, b->split_solve);
         if (e == cudaSuccess) e = cudaEventRecord(e1, s);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[part], e0, e1);

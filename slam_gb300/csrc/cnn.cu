@@ -563,11 +563,13 @@ cudaError_t cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M
                            int *err, cudaStream_t s) {
     const LdDense la{A, M, K, (K + 7) & ~7}, lb{B, N, K, (K + 7) & ~7};
     const EpStore ep{C, N, N};
-    if (layout == 2) {  // FP16 operands
-        if (bn == 32) return launch_umma_gemm<32, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
-        if (bn == 64) return launch_umma_gemm<64, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
-        if (bn == 128) return launch_umma_gemm<128, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
-        return launch_umma_gemm<256, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, 0, err, s);
+    if ((layout & 3) == 2) {  // FP16 operands
+        const int lay = layout & 4;
+        if (bn == 32) return launch_umma_gemm<32, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, lay, err, s);
+        if (bn == 64) return launch_umma_gemm<64, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, lay, err, s);
+        if (bn == 128)
+            return launch_umma_gemm<128, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, lay, err, s);
+        return launch_umma_gemm<256, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, lay, err, s);
     }
     if (bn == 32) return launch_umma_gemm<32>(la, lb, ep, M, N, K, 1, layout, err, s);
     if (bn == 64) return launch_umma_gemm<64>(la, lb, ep, M, N, K, 1, layout, err, s);

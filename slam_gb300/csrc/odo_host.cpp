@@ -92,6 +92,9 @@ struct odo_handle {
     int parity = 0;  // nextImage = parity ? imgB : imgA, lastNextImage = the other
     int mode = ODO_MODE_GRAPH;
     int precision = ODO_PREC_FP32;
+    // bounded waits of the persistent kernel (odo_debug_set_wait_limit)
+    long long spin_limit = kPersistentSpinLimit;
+    int absent_block = -1;
     TrackLaunch cfg[kLevels];
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::string last_error;
@@ -171,7 +174,6 @@ cudaError_t enqueue_derivatives(odo_t *h, cudaStream_t s) {
 
 LevelArgs level_args(odo_t *h, int l) {
     LevelArgs L{};
-    L.prefetch = g_l2_prefetch;  // all of the handle's buffers are its own
     L.level = l;
     L.cols = h->dims_w[l];
     L.rows = h->dims_h[l];
@@ -247,7 +249,8 @@ cudaError_t enqueue_track(odo_t *h, const int iterations[kLevels], int icp, int 
         if (!rgb) c.blocks_rgb = 1;
         if (h->mode == ODO_MODE_PERSISTENT) {
             if ((e = cudaMemsetAsync(h->ws.counters, 0, 4 * sizeof(unsigned), s)) != cudaSuccess) return e;
-            if ((e = launch_level_persistent(L, h->st_dev, h->ws, c, iterations[l], h->sm_count, s)) != cudaSuccess)
+            if ((e = launch_level_persistent(L, h->st_dev, h->ws, c, iterations[l], h->sm_count, s, h->spin_limit,
+                                             h->absent_block)) != cudaSuccess)
                 return e;
         } else {
             for (int j = 0; j < iterations[l]; ++j)
@@ -699,13 +702,10 @@ int odo_debug_history(odo_t *h, double *out, int max_rows) {
     return n;
 }
 
-int odo_debug_set_prefetch(int on) {
-    g_l2_prefetch = on ? 1 : 0;
-    return ODO_OK;
-}
-
-int odo_batch_debug_set_split(int on) {
-    g_split_solve = on ? 1 : 0;
+int odo_debug_set_wait_limit(odo_t *h, long long polls, int absent_block) {
+    if (!h || polls < 1 || absent_block < -1) return ODO_ERR_ARG;
+    h->spin_limit = polls;
+    h->absent_block = absent_block;
     return ODO_OK;
 }
 

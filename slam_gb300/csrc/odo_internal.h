@@ -99,7 +99,6 @@ struct LevelArgs {
     Img<const uint8_t> lastImage, nextImage;
     Img<Corr> corr;
     Img<const uint8_t> cand;  // pose-independent photometric preconditions, per pixel
-    int prefetch;             // 1: every buffer above is the library's own (L2 bulk prefetch allowed)
     float minScale;
     float maxDepthDelta;
     float sobelScale;
@@ -219,8 +218,11 @@ cudaError_t launch_track_begin(TrackState *st, cudaStream_t s);
 cudaError_t launch_so3(TrackState *st, Img<const uint8_t> last, Img<const uint8_t> next, Intr K2, cudaStream_t s);
 cudaError_t launch_level_iteration(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg, int iter,
                                    cudaStream_t s);
+// grid barriers of the persistent kernel give up after this many polls
+constexpr long long kPersistentSpinLimit = 1ll << 26;
 cudaError_t launch_level_persistent(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg,
-                                    int iterations, int sm_count, cudaStream_t s);
+                                    int iterations, int sm_count, cudaStream_t s,
+                                    long long spin_limit = kPersistentSpinLimit, int absent = -1);
 cudaError_t launch_track_end(TrackState *st, cudaStream_t s);
 cudaError_t launch_iteration_part(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg, int iter,
                                   int which, cudaStream_t s);
@@ -236,12 +238,8 @@ cudaError_t launch_track_end_batch(TrackState *states, int npairs, cudaStream_t 
 cudaError_t launch_so3_batch(const So3Args *args, int npairs, cudaStream_t s);
 // parts: bit 0 the association/residual kernel, bit 1 the photometric/solve kernel
 cudaError_t launch_level_iteration_batch(const PassArgs *args, int npairs, int max_nb_icp, int max_nb_rgb,
-                                         int threads, int precision, int iter, cudaStream_t s, int parts = 3);
-
-// process-wide switch of the iteration kernels' L2 bulk prefetch (default off)
-extern int g_l2_prefetch;
-// process-wide switch: batched photometric pass and solve as two kernels (default on)
-extern int g_split_solve;
+                                         int threads, int precision, int iter, cudaStream_t s, int parts = 3,
+                                         int split_solve = 1);
 
 // debug single passes
 cudaError_t launch_debug_icp(const LevelArgs &L, const float Rcurr[9], const float tcurr[3], const float Rprev_inv[9],

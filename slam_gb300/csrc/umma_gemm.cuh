@@ -28,14 +28,19 @@ namespace slamgb {
 constexpr int kGemmThreads = 128;
 constexpr int kGemmKChunk = 64;
 constexpr uint32_t kGemmWaitPolls = 1u << 22;
+// polls of the failure-detection test's wait on a barrier nothing arrives at
+constexpr uint32_t kGemmStallTestPolls = 256;
 
 template <int BN>
 constexpr int gemm_smem_bytes() {
     return 2 * (128 * kGemmKChunk * 2 + BN * kGemmKChunk * 2) + 1024;
 }
 
-// `layout` selects the operand core-matrix offsets (0: K-direction 128 B,
-// row-direction 1024 B; 1: the two exchanged) for the layout self-check.
+// `layout` bits 0-1 select the operand core-matrix offsets (0: K-direction
+// 128 B, row-direction 1024 B; 1: the two exchanged) for the layout
+// self-check; bit 2 (failure-detection test) makes the first pipeline wait
+// wait on an mbarrier that nothing arrives at, so that it runs out, the MMAs
+// already issued are drained and the kernel reports a time-out.
 // F16: the loaders return FP16 instead of BF16 values.
 template <int BN, bool F16, class LA, class LB, class EP>
 __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep, int M, int N, int kchunks,
@@ -44,7 +49,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
     constexpr int A_BYTES = 128 * kGemmKChunk * 2, B_BYTES = BN * kGemmKChunk * 2, STAGE = A_BYTES + B_BYTES;
     constexpr uint32_t IDESC = F16 ? umma::idesc_f16_f32(128, BN) : umma::idesc_bf16_f32(128, BN);
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar[3];
     __shared__ uint32_t tmem_base;
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -53,6 +58,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
     const int c_end = min(kchunks, c_begin + chunks_per_split);
     const int nch = c_end - c_begin;
     if (nch <= 0) return;
+    const bool stall_test = (layout & 4) != 0;
+    layout &= 3;
     if (warp == 0) {
         umma::tmem_alloc(&tmem_base, BN < 32 ? 32 : BN);
         umma::tmem_relinquish();
@@ -60,6 +67,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
     if (tid == 0) {
         umma::mbar_init(&mbar[0], 1);
         umma::mbar_init(&mbar[1], 1);
+        umma::mbar_init(&mbar[2], 1);  // never arrived at (stall test)
         umma::mbar_fence_init();
     }
     umma::fence_before_sync();
@@ -86,7 +94,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
         // the MMAs of chunk c - 2 read this stage; the decision to go on is
         // block-uniform so every thread leaves the loop at the same chunk
         if (c >= 2) {
-            ok = umma::mbar_wait(&mbar[s], ((c - 2) >> 1) & 1, kGemmWaitPolls);
+            ok = stall_test ? umma::mbar_wait(&mbar[2], 0, kGemmStallTestPolls)
+                            : umma::mbar_wait(&mbar[s], ((c - 2) >> 1) & 1, kGemmWaitPolls);
             if (!__syncthreads_and(ok)) break;
         }
         const int k8 = (c_begin + c) * (kGemmKChunk / 8) + kg;
@@ -112,10 +121,12 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
             umma::mma_commit(&mbar[s]);
         }
     }
-    // all MMAs issued so far are done when the last commit's phase completes
+    // all MMAs issued so far are done when the last commit's phase
+    // completes; waited for (bounded) whatever stopped the loop, so that no
+    // MMA still writes the accumulator when TMEM is released
     const int last = c - 1;
-    ok = ok && umma::mbar_wait(&mbar[last & 1], (last >> 1) & 1, kGemmWaitPolls);
-    ok = __syncthreads_and(ok) && c == nch;
+    const bool drained = umma::mbar_wait(&mbar[last & 1], (last >> 1) & 1, kGemmWaitPolls);
+    ok = __syncthreads_and(ok && drained) && c == nch;
     umma::fence_after_sync();
     if (ok) {
         const int row = m0 + warp * 32 + lane;

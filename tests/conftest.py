@@ -13,6 +13,19 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
 
 
+# Tolerances the parity tests applied and the errors they measured (one line
+# per check), printed at the end of the run so that a widened tolerance is
+# visible in the log of a passing run.
+TOLERANCE_REPORT = []
+
+
+def pytest_terminal_summary(terminalreporter):
+    if TOLERANCE_REPORT:
+        terminalreporter.section("parity tolerances applied")
+        for line in TOLERANCE_REPORT:
+            terminalreporter.write_line(line)
+
+
 def has_gpu():
     try:
         import torch

@@ -1,7 +1,15 @@
 """Shared helpers of the GPU parity tests."""
 import numpy as np
 
-from conftest import ANGLE_THRESH, DIST_THRESH
+from conftest import ANGLE_THRESH, DIST_THRESH, TOLERANCE_REPORT
+
+# Pose tolerance against the oracle: 1e-5 rad / 1e-5 m, the bound the
+# reference path is held to.  It is widened only for inputs on which the
+# reference algorithm itself does not determine the pose to that precision:
+# where the oracle's FP32 and FP64 runs differ by GAP_LIMIT or more.
+POSE_TOL_RAD = 1e-5
+POSE_TOL_M = 1e-5
+GAP_LIMIT = 5e-6
 
 
 def dev(a):
@@ -77,3 +85,90 @@ def rel_close(a, b, rtol):
     b = np.asarray(b, np.float64)
     scale = max(np.abs(b).max(), 1e-30)
     return np.abs(a - b).max() <= rtol * scale, float(np.abs(a - b).max() / scale)
+
+
+def report(line):
+    TOLERANCE_REPORT.append(line)
+    print(line)
+
+
+# The integer images of the photometric term (intensity pyramids, derivative
+# images).  Their kernels make rounding decisions -- truncations of quotients
+# and weighted sums -- that the reference takes with its approximate
+# division; the CPU oracle takes them with IEEE arithmetic and differs on tie
+# pixels.  Ours match the reference's kernels bit for bit
+# (test_gpu_reference.py), so whole-tracking comparisons give the oracle's
+# host loop these images from the GPU: what remains between the two is the
+# tracking loop itself.
+IMAGE_BUFFERS = (("lastImage", 7), ("nextImage", 8), ("lastNextImage", 9), ("dIdx", 10), ("dIdy", 11))
+
+
+def gpu_images(g):
+    """The reference-exact integer images of a loaded GPU handle (derivatives
+    computed from its nextImage, as the tracking call does)."""
+    g.debug_derivatives()
+    return {(name, l): g.download(which, l) for name, which in IMAGE_BUFFERS for l in range(3)}
+
+
+def pair_images(pair, first=True):
+    """gpu_images of a frame pair loaded on a fresh GPU handle."""
+    g = new_gpu_odo(pair["cam"])
+    load_frame(g, pair, first)
+    out = gpu_images(g)
+    g.close()
+    return out
+
+
+def set_images(o, images):
+    for (name, l), a in images.items():
+        o.set_buffer(name, l, a)
+    o.keep_derivatives(True)
+
+
+def oracle_track(pair, flags, levels=0, iterations=(0, 0, 0), prec=32, first=True, images=None):
+    """The oracle's host loop on one pair (with the batched tracker's per-pair
+    schedule when levels > 0), on the GPU's integer images when given.
+    Returns (t, R, oracle handle)."""
+    o = new_oracle_odo(pair["cam"], prec)
+    if levels:
+        o.set_schedule(levels, iterations)
+    load_frame(o, pair, first)
+    if images is not None:
+        set_images(o, images)
+    t, R = track(o, pair, **flags)
+    return t, R, o
+
+
+def pose_tolerance(pair, t32, R32, o32, flags, levels=0, iterations=(0, 0, 0), first=True, images=None):
+    """(tol_rad, tol_m, how): flat 1e-5 where the FP32 oracle and its FP64
+    twin agree to GAP_LIMIT; otherwise twice the precision to which the
+    reference algorithm determines the pose on this input -- the FP32/FP64
+    gap or the size of the last Gauss-Newton increment (an iteration that has
+    not converged leaves the pose undetermined to about one step), whichever
+    is larger."""
+    t64, R64, _ = oracle_track(pair, flags, levels, iterations, prec=64, first=first, images=images)
+    gap = pose_diff(t32, R32, t64, R64)
+    if gap[0] < GAP_LIMIT and gap[1] < GAP_LIMIT:
+        return POSE_TOL_RAD, POSE_TOL_M, "flat (fp32/fp64 gap %.1e rad %.1e m)" % gap
+    rot, tr = gap
+    hist = o32.history()
+    if len(hist):
+        rot = max(rot, float(np.linalg.norm(hist[-1][6:9])))
+        tr = max(tr, float(np.linalg.norm(hist[-1][3:6])))
+    return (max(POSE_TOL_RAD, 2 * rot), max(POSE_TOL_M, 2 * tr),
+            "widened (fp32/fp64 gap %.1e rad %.1e m, last step %.1e rad %.1e m)" % (gap[0], gap[1], rot, tr))
+
+
+def check_pose(label, tg, Rg, to, Ro, tol_fn):
+    """Asserts that the GPU pose is within tolerance of the oracle's and
+    records the tolerance applied.  A pose within the flat 1e-5 bound passes
+    as it is; otherwise tol_fn() -> (tol_rad, tol_m, how) gives the bound for
+    this input (pose_tolerance)."""
+    rot, tr = pose_diff(tg, Rg, to, Ro)
+    if rot <= POSE_TOL_RAD and tr <= POSE_TOL_M:
+        report("%s: pose diff %.2e rad %.2e m <= flat 1e-5" % (label, rot, tr))
+        return rot, tr, True
+    tol_r, tol_t, how = tol_fn()
+    report("%s: pose diff %.2e rad %.2e m, tolerance %.2e rad %.2e m %s" % (label, rot, tr, tol_r, tol_t, how))
+    assert rot <= tol_r and tr <= tol_t, (label, rot, tr, tol_r, tol_t, how)
+    return rot, tr, False

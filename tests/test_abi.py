@@ -46,3 +46,18 @@ def test_argument_validation_without_gpu(built):
     assert L.odo_get_stats(None, None) == 1
     assert L.odo_status_string(0) == b"ok"
     assert L.odo_status_string(5) == b"device-side wait timed out"
+
+
+def test_default_thresholds_match_reference_expression():
+    """ODO_DEFAULT_ANGLE_THRESH is sin(20.f * 3.14159254f / 180.f) rounded to
+    float, as the reference evaluates its default (src/odom/RGBDOdometryef.h:36),
+    bit for bit; the Python side uses the same value."""
+    import re
+    import numpy as np
+    from slam_gb300 import DEFAULT_ANGLE_THRESH, DEFAULT_DIST_THRESH
+    hdr = open(os.path.join(ROOT, "include", "slam_gb300.h")).read()
+    ang = float(re.search(r"#define ODO_DEFAULT_ANGLE_THRESH ([0-9.]+)f", hdr).group(1))
+    dist = float(re.search(r"#define ODO_DEFAULT_DIST_THRESH ([0-9.]+)f", hdr).group(1))
+    x = np.float32(np.float32(20.0) * np.float32(3.14159254)) / np.float32(180.0)
+    assert np.float32(ang) == np.float32(np.sin(np.float64(x))) == np.float32(DEFAULT_ANGLE_THRESH)
+    assert np.float32(dist) == np.float32(0.10) == np.float32(DEFAULT_DIST_THRESH)

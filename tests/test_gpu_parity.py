@@ -10,13 +10,11 @@ import numpy as np
 import pytest
 
 from conftest import ANGLE_THRESH, DIST_THRESH
-from gpu_helpers import (corr_to_dataterm, dev, intr, load_frame, new_gpu_odo, new_oracle_odo, pose_diff,
-                         rel_close, track)
+from gpu_helpers import (POSE_TOL_M, POSE_TOL_RAD, check_pose, corr_to_dataterm, dev, gpu_images, intr, load_frame,
+                         new_gpu_odo, new_oracle_odo, oracle_track, pose_diff, pose_tolerance, rel_close, set_images,
+                         track)
 
 pytestmark = pytest.mark.gpu
-
-POSE_TOL_RAD = 1e-5
-POSE_TOL_M = 1e-5
 
 
 @pytest.fixture(scope="module")
@@ -25,10 +23,13 @@ def orc(built):
     return oracle
 
 
-@pytest.fixture(scope="module")
-def pair640(gpu):
+@pytest.fixture(scope="module", params=[(640, 480), (90, 66), (80, 60)], ids=["640x480", "90x66", "80x60"])
+def pair640(gpu, request):
+    """The per-kernel parity pair: 640x480 (the reference's configuration)
+    and two small sizes whose coarsest level is a few hundred pixels."""
     from slam_gb300 import synth
-    return synth.make_pair(3)
+    w, h = request.param
+    return synth.make_pair(3, cam=synth.Camera().scaled(w, h))
 
 
 @pytest.fixture(scope="module")
@@ -176,7 +177,7 @@ def test_rgb_residual_and_step(loaded, orc, pair640, level):
                                               (corr_g[..., 1] != corres_e["zero_y"]) |
                                               (corr_g[..., 2] != corres_e["diff"].astype(np.int16))))
     assert np.all(tie[mism] != 0), (level, int(mism.sum()), int((mism & (tie == 0)).sum()))
-    assert valid_e.sum() > 100
+    assert valid_e.sum() > 0.01 * valid_e.size
     if not mism.any():
         assert (cnt_g, sig_g) == (cnt_e, sig_e)
     # photometric reduction on the GPU's correspondences
@@ -215,34 +216,6 @@ FLAGS = [
 ]
 
 
-def fp32_noise(pair, **flags):
-    """How precisely the reference algorithm determines the pose on this
-    input: (a) how far it moves between FP32 and FP64 (oracle vs its FP64
-    twin), (b) the size of its last Gauss-Newton increment (an iteration that
-    has not converged, or oscillates, leaves the pose undetermined to about
-    one step).  Two FP32 implementations that sum in different orders, or
-    round one tie differently, can differ by this much."""
-    o32 = new_oracle_odo(pair["cam"], 32)
-    load_frame(o32, pair)
-    t32, R32 = track(o32, pair, **flags)
-    o64 = new_oracle_odo(pair["cam"], 64)
-    load_frame(o64, pair)
-    t64, R64 = track(o64, pair, **flags)
-    rot, tr = pose_diff(t32, R32, t64, R64)
-    hist = o32.history()
-    if len(hist):
-        last = hist[-1]
-        rot = max(rot, float(np.linalg.norm(last[6:9])))
-        tr = max(tr, float(np.linalg.norm(last[3:6])))
-    return (t32, R32, o32), (rot, tr)
-
-
-def pose_tolerance(noise):
-    """1e-5 rad / 1e-5 m, widened to twice the precision to which the
-    reference algorithm itself determines the pose on this input."""
-    return max(POSE_TOL_RAD, 2 * noise[0]), max(POSE_TOL_M, 2 * noise[1])
-
-
 @pytest.mark.parametrize("seed", [3, 8])
 @pytest.mark.parametrize("flags", FLAGS, ids=lambda f: ",".join(f"{k}={v}" for k, v in f.items()) or "default")
 def test_tracking_matches_oracle(gpu, orc, seed, flags):
@@ -250,11 +223,11 @@ def test_tracking_matches_oracle(gpu, orc, seed, flags):
     pair = synth.make_pair(seed)
     g = new_gpu_odo(pair["cam"])
     load_frame(g, pair)
+    images = gpu_images(g)
     tg, Rg = track(g, pair, **flags)
-    (to, Ro, o), noise = fp32_noise(pair, **flags)
-    rot, tr = pose_diff(tg, Rg, to, Ro)
-    tol_r, tol_t = pose_tolerance(noise)
-    assert rot <= tol_r and tr <= tol_t, (rot, tr, noise, g.iterations(), o.iterations())
+    to, Ro, o = oracle_track(pair, flags, images=images)
+    label = "tracking seed %d %s" % (seed, ",".join(f"{k}={v}" for k, v in flags.items()) or "default")
+    check_pose(label, tg, Rg, to, Ro, lambda: pose_tolerance(pair, to, Ro, o, flags, images=images))
     assert g.iterations() == o.iterations()
     st = o.stats
     assert abs(g.lastICPCount - st["lastICPCount"]) <= 0.002 * max(1.0, st["lastICPCount"])
@@ -305,23 +278,37 @@ def test_sequence_with_image_swap(gpu, orc):
         T.append(T[-1] @ synth.random_motion(rng, 1.5, 0.03))
     g = new_gpu_odo(cam)
     o = new_oracle_odo(cam)
+    o64 = new_oracle_odo(cam, 64)
     first = synth.render(scene, T[0], cam, noise_seed=100)
     g.initFirstRGB(dev(first["rgba"]))
     o.initFirstRGB(first["rgba"])
+    o64.initFirstRGB(first["rgba"])
     pg = po = (T[0][:3, 3].astype(np.float32), T[0][:3, :3].astype(np.float32))
     for k in range(1, 4):
         model = synth.render(scene, T[k - 1], cam, depth=False, model=True)
         live = synth.render(scene, T[k], cam, noise_seed=100 + k)
         pair = {"cam": cam, "T1": T[k - 1], "model_vert": model["vert"], "model_norm": model["norm"],
                 "model_rgba": model["rgba"], "depth": live["depth"], "rgba": live["rgba"]}
-        load_frame(g, pair, first=False)
-        load_frame(o, pair, first=False)
-        pg = g.getIncrementalTransformation(pg[0], pg[1])
-        po = o.getIncrementalTransformation(po[0], po[1])
+        for odo in (g, o, o64):
+            load_frame(odo, pair, first=False)
+        images = gpu_images(g)
+        set_images(o, images)
+        set_images(o64, images)
+        start = po
+        pg = g.getIncrementalTransformation(start[0], start[1])
+        po = o.getIncrementalTransformation(start[0], start[1])
+        p64 = o64.getIncrementalTransformation(start[0], start[1])
         assert g.iterations() == o.iterations(), (k, g.iterations(), o.iterations())
-        rot, tr = pose_diff(np.float64(pg[0]), np.float64(pg[1]), np.float64(po[0]), np.float64(po[1]))
-        assert rot <= 3e-5 and tr <= 3e-5, (k, rot, tr)
-        pg = (np.float32(po[0]), np.float32(po[1]))  # continue both from the same pose
+
+        def tol(po=po, p64=p64):
+            gap = pose_diff(np.float64(po[0]), np.float64(po[1]), np.float64(p64[0]), np.float64(p64[1]))
+            if gap[0] < 5e-6 and gap[1] < 5e-6:
+                return POSE_TOL_RAD, POSE_TOL_M, "flat (fp32/fp64 gap %.1e rad %.1e m)" % gap
+            return max(POSE_TOL_RAD, 2 * gap[0]), max(POSE_TOL_M, 2 * gap[1]), "widened (fp32/fp64 gap)"
+        check_pose("sequence frame %d" % k, np.float64(pg[0]), np.float64(pg[1]), np.float64(po[0]),
+                   np.float64(po[1]), tol)
+        pg = (np.float32(po[0]), np.float32(po[1]))  # continue all three from the oracle's pose
+        po = pg
 
 
 @pytest.mark.parametrize("size", [(90, 66), (80, 60), (320, 240)])
@@ -331,12 +318,11 @@ def test_small_and_odd_sizes(gpu, orc, size):
     pair = synth.make_pair(4, cam=synth.Camera().scaled(w, h))
     g = new_gpu_odo(pair["cam"])
     load_frame(g, pair)
+    images = gpu_images(g)
     tg, Rg = track(g, pair)
-    (to, Ro, o), noise = fp32_noise(pair)
+    to, Ro, o = oracle_track(pair, {}, images=images)
     assert g.iterations() == o.iterations(), (size, g.iterations(), o.iterations())
-    rot, tr = pose_diff(tg, Rg, to, Ro)
-    tol_r, tol_t = pose_tolerance(noise)
-    assert rot <= tol_r and tr <= tol_t, (size, rot, tr, noise)
+    check_pose("size %dx%d" % size, tg, Rg, to, Ro, lambda: pose_tolerance(pair, to, Ro, o, {}, images=images))
 
 
 def test_tiny_image_runs(gpu):

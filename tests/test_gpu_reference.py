@@ -24,10 +24,11 @@ def ref(gpu):
     return ref_runner.RefKernels()
 
 
-@pytest.fixture(scope="module")
-def pair(gpu):
+@pytest.fixture(scope="module", params=[(640, 480), (90, 66), (80, 60)], ids=["640x480", "90x66", "80x60"])
+def pair(gpu, request):
     from slam_gb300 import synth
-    return synth.make_pair(6)
+    w, h = request.param
+    return synth.make_pair(6, cam=synth.Camera().scaled(w, h))
 
 
 @pytest.fixture(scope="module")
