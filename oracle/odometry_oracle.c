@@ -247,6 +247,37 @@ static inline int near_thr(double a, double t, double rel) {
 }
 #define TIE_REL 4e-6
 
+/* Tie flipping (test infrastructure): when set, every decision flagged as a
+ * tie -- a quotient rounded to an integer within TIE_REL of the half-way
+ * point, a threshold comparison within TIE_REL of the threshold -- is taken
+ * the other way.  The pose difference between a normal and a flipped run
+ * measures how much the tracking result depends on decisions the reference's
+ * approximate division may take differently from IEEE arithmetic. */
+static int g_flip_ties = 0;
+void ORC(set_flip_ties)(int on) { g_flip_ties = on; }
+
+/* __float2int_rn of a quotient, flagging (and, when flipping, reversing) a
+ * rounding that sits on a tie. */
+static inline int round_q(real q, int *tie) {
+    int r = f2i_rn(q);
+    if (near_half(q, TIE_REL, fabs((double)q) + 1.0)) {
+        *tie = 1;
+        if (g_flip_ties) {
+            const double fl = floor((double)q);
+            r = (r == (int)fl) ? (int)fl + 1 : (int)fl;
+        }
+    }
+    return r;
+}
+/* a comparison result, reversed when flipping and its operands are a tie */
+static inline int decide(int result, double a, double t, int *tie) {
+    if (near_thr(a, t, TIE_REL)) {
+        *tie = 1;
+        if (g_flip_ties) return !result;
+    }
+    return result;
+}
+
 /* ------------------------------------------------------------------ */
 /* Map kernels (src/odom/utils.cu)                                     */
 /* ------------------------------------------------------------------ */
@@ -419,18 +450,26 @@ static void products7(real *p, const real *row, real found) {
 /* Pairwise (cascade) sum of n records of ncomp values each (record stride
  * `stride`), leaves of up to 8 records summed in order.  Deterministic and
  * with O(log n) error growth, close to the GPU's tree reductions. */
+/* Summation-order perturbation (test infrastructure): when set, every
+ * pairwise sum visits its records in reverse order -- the same error
+ * structure in another order, as a GPU reduction tree of another shape. */
+static int g_reverse_sums = 0;
+void ORC(set_reverse_sums)(int on) { g_reverse_sums = on; }
+
 static void pairwise_sum(const real *v, int n, int stride, int ncomp, real *out) {
     if (n <= 8) {
         for (int k = 0; k < ncomp; ++k) out[k] = 0;
-        for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const int i = g_reverse_sums ? n - 1 - j : j;
             for (int k = 0; k < ncomp; ++k) out[k] += v[(size_t)i * stride + k];
+        }
         return;
     }
     real a[32], b[32];
     int m = n / 2;
     pairwise_sum(v, m, stride, ncomp, a);
     pairwise_sum(v + (size_t)m * stride, n - m, stride, ncomp, b);
-    for (int k = 0; k < ncomp; ++k) out[k] = a[k] + b[k];
+    for (int k = 0; k < ncomp; ++k) out[k] = g_reverse_sums ? b[k] + a[k] : a[k] + b[k];
 }
 
 /* ------------------------------------------------------------------ */
@@ -459,8 +498,9 @@ static int icp_search(const icp_args *a, int x, int y, v3 *n, v3 *d, v3 *s, int 
     v3 vcurr_cp = mv(&a->Rprev_inv, sub(vcurr_g, a->tprev));
     real qx = vcurr_cp.x * a->fx / vcurr_cp.z + a->cx;
     real qy = vcurr_cp.y * a->fy / vcurr_cp.z + a->cy;
-    int ux = f2i_rn(qx), uy = f2i_rn(qy);
-    if (near_half(qx, TIE_REL, fabs((double)qx) + 1.0) || near_half(qy, TIE_REL, fabs((double)qy) + 1.0)) *tie |= 1;
+    int tq = 0;
+    int ux = round_q(qx, &tq), uy = round_q(qy, &tq);
+    if (tq) *tie |= 1;
     if (ux < 0 || uy < 0 || ux >= a->cols || uy >= a->rows || vcurr_cp.z < 0) return 0;
     const size_t q = (size_t)uy * a->cols + ux;
     v3 vprev_g = mk(a->vmap_g_prev[q], a->vmap_g_prev[N + q], a->vmap_g_prev[2 * N + q]);
@@ -470,8 +510,11 @@ static int icp_search(const icp_args *a, int x, int y, v3 *n, v3 *d, v3 *s, int 
     real dist = norm3(sub(vprev_g, vcurr_g));
     real sine = norm3(cross(ncurr_g, nprev_g));
     *n = nprev_g; *d = vprev_g; *s = vcurr_g;
-    if (near_thr(dist, a->distThres, TIE_REL) || near_thr(sine, a->angleThres, TIE_REL)) *tie |= 2;
-    int ok = (sine < a->angleThres && dist <= a->distThres && !isnan_r(ncurr.x) && !isnan_r(nprev_g.x));
+    int tt = 0;
+    const int sine_ok = decide(sine < a->angleThres, sine, a->angleThres, &tt);
+    const int dist_ok = decide(dist <= a->distThres, dist, a->distThres, &tt);
+    if (tt) *tie |= 2;
+    int ok = (sine_ok && dist_ok && !isnan_r(ncurr.x) && !isnan_r(nprev_g.x));
     if (ok) *idx = (int)q;
     return ok;
 }
@@ -563,14 +606,16 @@ void ORC(rgb_residual)(real minScale, const int16_t *dIdx, const int16_t *dIdy, 
                         real td1 = d1 * (krkinv[6] * (real)x + krkinv[7] * (real)y + krkinv[8]) + kt[2];
                         real qu = (d1 * (krkinv[0] * (real)x + krkinv[1] * (real)y + krkinv[2]) + kt[0]) / td1;
                         real qv = (d1 * (krkinv[3] * (real)x + krkinv[4] * (real)y + krkinv[5]) + kt[1]) / td1;
-                        int u0 = f2i_rn(qu), v0 = f2i_rn(qv);
-                        if (near_half(qu, TIE_REL, fabs((double)qu) + 1.0) ||
-                            near_half(qv, TIE_REL, fabs((double)qv) + 1.0))
-                            tf |= 1;
+                        int tq = 0;
+                        int u0 = round_q(qu, &tq), v0 = round_q(qv, &tq);
+                        if (tq) tf |= 1;
                         if (u0 >= 0 && v0 >= 0 && u0 < cols && v0 < rows) {
                             real d0 = lastDepth[v0 * cols + u0];
-                            if (d0 > 0 && near_thr(ABS(td1 - d0), maxDepthDelta, TIE_REL)) tf |= 2;
-                            if (d0 > 0 && ABS(td1 - d0) <= maxDepthDelta && lastImage[v0 * cols + u0] != 0) {
+                            int tt = 0;
+                            const int near = d0 > 0 && decide(ABS(td1 - d0) <= maxDepthDelta, ABS(td1 - d0),
+                                                               maxDepthDelta, &tt);
+                            if (d0 > 0 && tt) tf |= 2;
+                            if (near && lastImage[v0 * cols + u0] != 0) {
                                 c.zero_x = (int16_t)u0; c.zero_y = (int16_t)v0;
                                 c.one_x = (int16_t)x; c.one_y = (int16_t)y;
                                 c.diff = (float)nextImage[y * cols + x] - (float)lastImage[v0 * cols + u0];
@@ -665,7 +710,8 @@ void ORC(so3_step)(const uint8_t *lastImage, const uint8_t *nextImage, int cols,
             real *acc = rb + (size_t)x * 11;
             v3 p = mk((real)x, (real)y, 1);
             v3 wp = mv(&Hm, p);
-            int wx = f2i_rn(wp.x / wp.z), wy = f2i_rn(wp.y / wp.z);
+            int tq = 0;
+            int wx = round_q(wp.x / wp.z, &tq), wy = round_q(wp.y / wp.z, &tq);
             int found = wx >= 1 && wx < cols - 1 && wy >= 1 && wy < rows - 1 && x >= 1 && x < cols - 1 && y >= 1 &&
                         y < rows - 1;
             real row[4] = {0, 0, 0, 0};

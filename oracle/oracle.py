@@ -217,6 +217,18 @@ class Kernels:
         return out
 
 
+def set_flip_ties(prec, on):
+    """Decisions flagged as rounding ties are taken the other way (the
+    per-pixel kernels and the tracking loop of the given precision)."""
+    Kernels(prec).f("set_flip_ties")(int(bool(on)))
+
+
+def set_reverse_sums(prec, on):
+    """Every pairwise sum of the given precision visits its records in reverse
+    order (a summation-order perturbation)."""
+    Kernels(prec).f("set_reverse_sums")(int(bool(on)))
+
+
 def ldlt_solve6(A, b):
     A = np.ascontiguousarray(A, np.float64).reshape(36)
     b = np.ascontiguousarray(b, np.float64).reshape(6)

@@ -4,15 +4,14 @@ Every pair of a mixed batch -- 160x120 / 320x240 / 640x480, 2 or 3 pyramid
 levels -- is compared with the oracle's host loop run with that pair's
 schedule (the reference's per-level iteration counts restricted to the pair's
 levels, src/odom/RGBDOdometryef.cpp:382-384): pose within the tolerance of
-gpu_helpers.pose_tolerance and identical iteration counts.  A full
+gpu_helpers.OracleRuns.tolerance and identical iteration counts.  A full
 512-pair batch of the batched-verification workload is checked the same way.
 Pairs with 3 levels are also bit-identical to the single-pair call on the same
 inputs (same kernels, same per-pair launch shape, same summation order)."""
 import numpy as np
 import pytest
 
-from gpu_helpers import (check_pose, dev, dev_u16, load_frame, new_gpu_odo, oracle_track, pair_images, pose_tolerance,
-                         report, track)
+from gpu_helpers import check_pose, dev, dev_u16, frame_runs, load_frame, new_gpu_odo, pair_images, report, track
 
 pytestmark = pytest.mark.gpu
 
@@ -42,23 +41,25 @@ def to_batch(pairs):
 
 def check_against_oracle(pairs, res, flags, tag):
     from slam_gb300.batch import result_pose
-    flat = 0
+    flat = undetermined = 0
     worst = (0.0, 0.0)
     for i, p in enumerate(pairs):
-        images = pair_images(p)
-        to, Ro, o = oracle_track(p, flags, levels=p["levels"], images=images)
+        ref = frame_runs(p, flags, levels=p["levels"], images=pair_images(p))
+        to, Ro, o = ref.main
         T = result_pose(res[i])
         label = "%s pair %d %dx%d levels %d" % (tag, i, p["cam"].width, p["cam"].height, p["levels"])
-        rot, tr, is_flat = check_pose(label, T[:3, 3], T[:3, :3], to, Ro,
-                                      lambda: pose_tolerance(p, to, Ro, o, flags, levels=p["levels"], images=images))
+        rot, tr, is_flat = check_pose(label, T[:3, 3], T[:3, :3], to, Ro, ref.tolerance)
+        if not is_flat and ref.undetermined():
+            undetermined += 1
+            continue
         flat += is_flat
         worst = (max(worst[0], rot), max(worst[1], tr))
         assert list(res[i].iterations) == o.iterations(), (label, list(res[i].iterations), o.iterations())
         st = o.stats
         assert abs(res[i].lastICPCount - st["lastICPCount"]) <= 0.002 * max(1.0, st["lastICPCount"]), label
         assert abs(res[i].lastRGBCount - st["lastRGBCount"]) <= 0.002 * max(1.0, st["lastRGBCount"]), label
-    report("%s: %d/%d pairs within the flat 1e-5 bound, max pose diff %.2e rad %.2e m"
-           % (tag, flat, len(pairs), worst[0], worst[1]))
+    report("%s: %d/%d pairs within the flat 1e-5 bound, %d undetermined by the reference algorithm, max pose "
+           "diff of the others %.2e rad %.2e m" % (tag, flat, len(pairs), undetermined, worst[0], worst[1]))
 
 
 FLAGS = [dict(), dict(so3=False), dict(icpWeight=100.0, so3=False), dict(rgbOnly=True, so3=False)]

@@ -20,8 +20,8 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
-from gpu_helpers import (check_pose, dev, gpu_images, new_gpu_odo, new_oracle_odo, oracle_track, pair_images,
-                         pose_diff, pose_tolerance, rel_close, report, set_images, track)
+from gpu_helpers import (OracleRuns, check_pose, dev, frame_runs, gpu_images, new_gpu_odo, pair_images, rel_close,
+                         report, set_images, track)
 
 pytestmark = pytest.mark.gpu
 
@@ -120,22 +120,10 @@ def test_ferns_shaped_check_matches_oracle(gpu, seed):
     g = new_gpu_odo(pair["cam"])
     _load_maps(g, pair, rgb=False)
     tg, Rg = track(g, pair, **FERNS_FLAGS)
-    o = new_oracle_odo(pair["cam"])
-    _load_maps(o, pair, rgb=False)
-    to, Ro = track(o, pair, **FERNS_FLAGS)
-
-    def tol():
-        o64 = new_oracle_odo(pair["cam"], 64)
-        _load_maps(o64, pair, rgb=False)
-        t64, R64 = track(o64, pair, **FERNS_FLAGS)
-        gap = pose_diff(to, Ro, t64, R64)
-        last = o.history()[-1]
-        rot = max(gap[0], float(np.linalg.norm(last[6:9])))
-        tr = max(gap[1], float(np.linalg.norm(last[3:6])))
-        if gap[0] < 5e-6 and gap[1] < 5e-6:
-            return 1e-5, 1e-5, "flat"
-        return max(1e-5, 2 * rot), max(1e-5, 2 * tr), "widened"
-    check_pose("ferns 80x60 seed %d" % seed, tg, Rg, to, Ro, tol)
+    T1 = pair["T1"]
+    ref = OracleRuns(pair["cam"], lambda o: _load_maps(o, pair, rgb=False), (T1[:3, 3], T1[:3, :3]), FERNS_FLAGS)
+    to, Ro, o = ref.main
+    check_pose("ferns 80x60 seed %d" % seed, tg, Rg, to, Ro, ref.tolerance)
     assert g.iterations() == o.iterations() == [0, 10, 0, 0]
     st = o.stats
     assert g.lastICPCount == st["lastICPCount"]
@@ -161,22 +149,14 @@ def test_model_to_model_check_matches_oracle(gpu, seed):
     _load_maps(g, pair, rgb=True)
     images = gpu_images(g)
     tg, Rg = track(g, pair, **flags)
-    o = new_oracle_odo(pair["cam"])
-    _load_maps(o, pair, rgb=True)
-    set_images(o, images)
-    to, Ro = track(o, pair, **flags)
 
-    def tol():
-        o64 = new_oracle_odo(pair["cam"], 64)
-        _load_maps(o64, pair, rgb=True)
-        set_images(o64, images)
-        t64, R64 = track(o64, pair, **flags)
-        gap = pose_diff(to, Ro, t64, R64)
-        if gap[0] < 5e-6 and gap[1] < 5e-6:
-            return 1e-5, 1e-5, "flat"
-        last = o.history()[-1]
-        return (max(1e-5, 2 * max(gap[0], float(np.linalg.norm(last[6:9])))),
-                max(1e-5, 2 * max(gap[1], float(np.linalg.norm(last[3:6])))), "widened")
+    def load(o):
+        _load_maps(o, pair, rgb=True)
+        set_images(o, images)
+    T1 = pair["T1"]
+    ref = OracleRuns(pair["cam"], load, (T1[:3, 3], T1[:3, :3]), flags)
+    to, Ro, o = ref.main
+    tol = ref.tolerance
     check_pose("model-to-model 320x240 seed %d" % seed, tg, Rg, to, Ro, tol)
     assert g.iterations() == o.iterations()
     cg, co = g.getCovariance(), o.getCovariance()
@@ -300,10 +280,9 @@ def test_cpp_shim_tracking_call(gpu, tmp_path):
     icp_err, icp_cnt = (float(v) for v in lines[2].split())
     lastA = np.array(lines[3].split(), np.float64).reshape(6, 6)
     cov = np.array(lines[4].split(), np.float64).reshape(6, 6)
-    images = pair_images(pair)
-    to, Ro, o = oracle_track(pair, {}, images=images)
-    check_pose("C++ shim 320x240", tg, Rg, to, Ro,
-               lambda: pose_tolerance(pair, to, Ro, o, dict(), images=images))
+    ref = frame_runs(pair, {}, images=pair_images(pair))
+    to, Ro, o = ref.main
+    check_pose("C++ shim 320x240", tg, Rg, to, Ro, ref.tolerance)
     st = o.stats
     assert abs(icp_cnt - st["lastICPCount"]) <= 0.002 * st["lastICPCount"]
     ok, err = rel_close(lastA, st["lastA"], 1e-3)

@@ -15,7 +15,7 @@ import ctypes
 
 import pytest
 
-from gpu_helpers import check_pose, gpu_images, load_frame, new_gpu_odo, oracle_track, pose_tolerance, track
+from gpu_helpers import check_pose, frame_runs, gpu_images, load_frame, new_gpu_odo, track
 
 pytestmark = pytest.mark.gpu
 
@@ -38,9 +38,9 @@ def test_persistent_barrier_times_out_and_handle_recovers(gpu):
     load_frame(g, pair)
     images = gpu_images(g)
     tg, Rg = track(g, pair)
-    to, Ro, o = oracle_track(pair, {}, images=images)
-    check_pose("persistent after time-out", tg, Rg, to, Ro,
-               lambda: pose_tolerance(pair, to, Ro, o, {}, images=images))
+    ref = frame_runs(pair, {}, images=images)
+    to, Ro, o = ref.main
+    check_pose("persistent after time-out", tg, Rg, to, Ro, ref.tolerance)
     assert L.odo_debug_set_wait_limit(g.handle, 0, -1) == 1  # bad limit refused
 
 

@@ -10,8 +10,8 @@ import numpy as np
 import pytest
 
 from conftest import ANGLE_THRESH, DIST_THRESH
-from gpu_helpers import (POSE_TOL_M, POSE_TOL_RAD, check_pose, corr_to_dataterm, dev, gpu_images, intr, load_frame,
-                         new_gpu_odo, new_oracle_odo, oracle_track, pose_diff, pose_tolerance, rel_close, set_images,
+from gpu_helpers import (POSE_TOL_M, POSE_TOL_RAD, OracleRuns, check_pose, corr_to_dataterm, dev, frame_runs,
+                         gpu_images, intr, load_frame, new_gpu_odo, new_oracle_odo, pose_diff, rel_close, set_images,
                          track)
 
 pytestmark = pytest.mark.gpu
@@ -225,14 +225,15 @@ def test_tracking_matches_oracle(gpu, orc, seed, flags):
     load_frame(g, pair)
     images = gpu_images(g)
     tg, Rg = track(g, pair, **flags)
-    to, Ro, o = oracle_track(pair, flags, images=images)
+    ref = frame_runs(pair, flags, images=images)
+    to, Ro, o = ref.main
     label = "tracking seed %d %s" % (seed, ",".join(f"{k}={v}" for k, v in flags.items()) or "default")
-    check_pose(label, tg, Rg, to, Ro, lambda: pose_tolerance(pair, to, Ro, o, flags, images=images))
+    _, _, flat = check_pose(label, tg, Rg, to, Ro, ref.tolerance)
     assert g.iterations() == o.iterations()
     st = o.stats
     assert abs(g.lastICPCount - st["lastICPCount"]) <= 0.002 * max(1.0, st["lastICPCount"])
     assert abs(g.lastRGBCount - st["lastRGBCount"]) <= 0.002 * max(1.0, st["lastRGBCount"])
-    ok, err = rel_close(g.lastA, st["lastA"], 1e-3)
+    ok, err = rel_close(g.lastA, st["lastA"], ref.jtj_tolerance(flat))
     assert ok, err
 
 
@@ -278,37 +279,30 @@ def test_sequence_with_image_swap(gpu, orc):
         T.append(T[-1] @ synth.random_motion(rng, 1.5, 0.03))
     g = new_gpu_odo(cam)
     o = new_oracle_odo(cam)
-    o64 = new_oracle_odo(cam, 64)
     first = synth.render(scene, T[0], cam, noise_seed=100)
     g.initFirstRGB(dev(first["rgba"]))
     o.initFirstRGB(first["rgba"])
-    o64.initFirstRGB(first["rgba"])
-    pg = po = (T[0][:3, 3].astype(np.float32), T[0][:3, :3].astype(np.float32))
+    start = (T[0][:3, 3].astype(np.float32), T[0][:3, :3].astype(np.float32))
     for k in range(1, 4):
         model = synth.render(scene, T[k - 1], cam, depth=False, model=True)
         live = synth.render(scene, T[k], cam, noise_seed=100 + k)
         pair = {"cam": cam, "T1": T[k - 1], "model_vert": model["vert"], "model_norm": model["norm"],
                 "model_rgba": model["rgba"], "depth": live["depth"], "rgba": live["rgba"]}
-        for odo in (g, o, o64):
-            load_frame(odo, pair, first=False)
-        images = gpu_images(g)
+        load_frame(g, pair, first=False)
+        load_frame(o, pair, first=False)
+        images = gpu_images(g)  # includes the swapped lastNextImage
         set_images(o, images)
-        set_images(o64, images)
-        start = po
         pg = g.getIncrementalTransformation(start[0], start[1])
         po = o.getIncrementalTransformation(start[0], start[1])
-        p64 = o64.getIncrementalTransformation(start[0], start[1])
         assert g.iterations() == o.iterations(), (k, g.iterations(), o.iterations())
 
-        def tol(po=po, p64=p64):
-            gap = pose_diff(np.float64(po[0]), np.float64(po[1]), np.float64(p64[0]), np.float64(p64[1]))
-            if gap[0] < 5e-6 and gap[1] < 5e-6:
-                return POSE_TOL_RAD, POSE_TOL_M, "flat (fp32/fp64 gap %.1e rad %.1e m)" % gap
-            return max(POSE_TOL_RAD, 2 * gap[0]), max(POSE_TOL_M, 2 * gap[1]), "widened (fp32/fp64 gap)"
+        def load(h, pair=pair, images=images):
+            load_frame(h, pair, first=False)
+            set_images(h, images)
+        ref = OracleRuns(cam, load, start, {})
         check_pose("sequence frame %d" % k, np.float64(pg[0]), np.float64(pg[1]), np.float64(po[0]),
-                   np.float64(po[1]), tol)
-        pg = (np.float32(po[0]), np.float32(po[1]))  # continue all three from the oracle's pose
-        po = pg
+                   np.float64(po[1]), ref.tolerance)
+        start = (np.float32(po[0]), np.float32(po[1]))  # continue both from the oracle's pose
 
 
 @pytest.mark.parametrize("size", [(90, 66), (80, 60), (320, 240)])
@@ -320,9 +314,10 @@ def test_small_and_odd_sizes(gpu, orc, size):
     load_frame(g, pair)
     images = gpu_images(g)
     tg, Rg = track(g, pair)
-    to, Ro, o = oracle_track(pair, {}, images=images)
+    ref = frame_runs(pair, {}, images=images)
+    to, Ro, o = ref.main
     assert g.iterations() == o.iterations(), (size, g.iterations(), o.iterations())
-    check_pose("size %dx%d" % size, tg, Rg, to, Ro, lambda: pose_tolerance(pair, to, Ro, o, {}, images=images))
+    check_pose("size %dx%d" % size, tg, Rg, to, Ro, ref.tolerance)
 
 
 def test_tiny_image_runs(gpu):
