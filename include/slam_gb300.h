@@ -175,6 +175,14 @@ typedef struct {
     const uint8_t *prev_rgba;    /* previous live RGBA for the SO3 stage (may be NULL when so3 = 0) */
     size_t prev_rgba_pitch;
     float pose[16];              /* model pose = starting pose, row-major camera-to-world */
+    /* Live side as camera-frame RGBA32F vertex / normal maps instead of a
+     * depth image: initICP(verts, norms) (src/odom/RGBDOdometryef.cpp:144-167)
+     * in place of initICP(depth).  When set, `depth` is not read and the live
+     * photometric depth comes from these vertices (as the reference's
+     * initRGB after initICP(verts, norms) does); NULL: depth input.  All
+     * pairs of one call use the same kind of live input. */
+    const float *live_verts, *live_norms;
+    size_t live_pitch;
 } odo_pair;
 
 typedef struct {
@@ -202,6 +210,31 @@ int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOn
  * counterpart in the reference; used by the learned warm start). */
 int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init_dev, int rgbOnly,
                          float icpWeight, int fastOdom, odo_pair_result *results);
+/* Loop-closure verification of candidate pairs, as the reference's callers
+ * decide it after one tracking call each:
+ *  - Ferns::findFrame (src/lc/Ferns.cpp:253-279): ICP only (icpWeight 100),
+ *    no pyramid (levels = 1), no SO3, live side as maps; accept when
+ *    lastICPError < max_icp_error (3e-4) and lastICPCount > min_icp_count
+ *    (2400, or 1400 when tracking is lost);
+ *  - model-to-model (src/apps/elastic_fusion_file.cpp:462-498): ICP + RGB
+ *    (icpWeight 10), pyramid, no SO3; accept when every diagonal entry of
+ *    getCovariance() is <= max_covariance (covThresh 1e-5),
+ *    lastICPCount > min_icp_count (icpCountThresh 40000) and
+ *    lastICPError < max_icp_error (icpErrThresh 5e-5).
+ * A test whose threshold is <= 0 is skipped.  All candidates run in one
+ * batched call (odo_batch_track); covariance (host, may be NULL) gets each
+ * pair's row-major 6x6 inverse of lastA, accept (host) 1 or 0 per pair. */
+typedef struct {
+    int rgbOnly;
+    float icpWeight;
+    int fastOdom;
+    int so3;
+    float max_icp_error;
+    float min_icp_count;
+    double max_covariance;
+} odo_verify_params;
+int odo_batch_verify(odo_batch_t *b, const odo_pair *pairs, int npairs, const odo_verify_params *vp,
+                     odo_pair_result *results, double *covariance, int *accept);
 /* Times every launch shape ({128, 256} threads x {2, 4, 8, 16, 32, 64} pixels
  * per thread) on these pairs, keeps the fastest and returns it. */
 int odo_batch_autotune(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,

@@ -65,7 +65,8 @@ class OdoPair(ctypes.Structure):
                 ("levels", c_int), ("iterations", c_int * 3), ("model_verts", c_void_p), ("model_norms", c_void_p), ("model_pitch", c_size_t),
                 ("model_rgba", c_void_p), ("model_rgba_pitch", c_size_t), ("depth", c_void_p),
                 ("depth_pitch", c_size_t), ("rgba", c_void_p), ("rgba_pitch", c_size_t), ("prev_rgba", c_void_p),
-                ("prev_rgba_pitch", c_size_t), ("pose", c_float * 16)]
+                ("prev_rgba_pitch", c_size_t), ("pose", c_float * 16), ("live_verts", c_void_p),
+                ("live_norms", c_void_p), ("live_pitch", c_size_t)]
 
 
 class OdoPairResult(ctypes.Structure):
@@ -73,6 +74,11 @@ class OdoPairResult(ctypes.Structure):
                 ("lastRGBError", c_float), ("lastRGBCount", c_float), ("lastSO3Error", c_float),
                 ("lastSO3Count", c_float), ("iterations", c_int * 4), ("done_us", c_double),
                 ("lastA", c_double * 36), ("lastb", c_double * 6)]
+
+
+class OdoVerifyParams(ctypes.Structure):
+    _fields_ = [("rgbOnly", c_int), ("icpWeight", c_float), ("fastOdom", c_int), ("so3", c_int),
+                ("max_icp_error", c_float), ("min_icp_count", c_float), ("max_covariance", c_double)]
 
 
 class OdoWarmParams(ctypes.Structure):
@@ -145,6 +151,7 @@ SIGNATURES = [
     ("odo_batch_track", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult)]),
     ("odo_batch_debug_time_iteration", c_int, [c_void_p, c_int, c_int, P(c_float)]),
     ("odo_batch_track_init", c_int, [c_void_p, P(OdoPair), c_int, c_void_p, c_int, c_float, c_int, P(OdoPairResult)]),
+    ("odo_batch_verify", c_int, [c_void_p, c_void_p, c_int, P(OdoVerifyParams), c_void_p, P(c_double), P(c_int)]),
     ("odo_batch_autotune", c_int, [c_void_p, P(OdoPair), c_int, c_int, c_float, c_int, c_int, P(OdoPairResult),
                                    P(c_int), P(c_int), P(c_float)]),
     ("odo_batch_last_error", ctypes.c_char_p, [c_void_p]),

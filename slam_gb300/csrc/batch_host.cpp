@@ -36,17 +36,18 @@ struct PairBufs {
     // device pointers (carved from the arena)
     Img<uint16_t> depth[kLevels];
     Map3 vc[kLevels], nc[kLevels], vp[kLevels], np[kLevels];
-    Img<float> dep[kLevels];  // photometric depth (last == next: both come from the model vertices)
+    Img<float> dep[kLevels];  // photometric depth (last, and next for depth input: both from the model vertices)
+    Img<float> depn[kLevels]; // next photometric depth for live maps input (from the live vertices)
     Img<uint8_t> last[kLevels], next[kLevels], lastnext[kLevels];
     Img<int16_t> dx[kLevels], dy[kLevels];
     Img<Corr> corr[kLevels];
     Img<uint8_t> cand[kLevels];
-    Img<float> vz;
+    Img<float> vz, vzn;  // raw vertex z of the model / live maps (level 0)
     ReduceWs ws;
 };
 
 using Layout = std::vector<std::tuple<int, int>>;
-using GKey = std::tuple<int, int, int, int, int, int, int, int, int, int>;
+using GKey = std::tuple<int, int, int, int, int, int, int, int, int, int, int>;
 
 }  // namespace
 
@@ -64,7 +65,7 @@ struct odo_batch {
     size_t args_bytes = 0;
     TrackState *st_dev = nullptr, *st_host = nullptr;           // host pinned
     // offsets of the argument blocks in the argument arena
-    size_t o_model, o_rgbd[3], o_gauss[3][2], o_pyr[2], o_vn, o_deriv, o_so3, o_pass[kLevels];
+    size_t o_model, o_live, o_rgbd[3], o_gauss[3][2], o_pyr[2], o_vn, o_deriv, o_so3, o_pass[kLevels];
     int threads = 256, ppt = 2;
     // 1: the last iteration stage is the photometric pass plus a
     // one-block-per-pair solve kernel (the pass then carries no FP64 solve
@@ -189,7 +190,9 @@ int ensure_layout(odo_batch_t *b, const odo_pair *pairs, int n) {
             carve_img<int16_t>(nul, off, w, h);
             carve_img<Corr>(nul, off, w, h);
             carve_img<uint8_t>(nul, off, w, h);
+            carve_img<float>(nul, off, w, h);
         }
+        carve_img<float>(nul, off, p.w, p.h);
         carve_img<float>(nul, off, p.w, p.h);
         off = round_up(off, 256) + round_up(sizeof(float) * 32 * maxb, 256) * 2 +
               round_up(sizeof(int) * 2 * maxb, 256) + 256;
@@ -219,8 +222,10 @@ int ensure_layout(odo_batch_t *b, const odo_pair *pairs, int n) {
             p.dy[l] = carve_img<int16_t>(base, off, w, h);
             p.corr[l] = carve_img<Corr>(base, off, w, h);
             p.cand[l] = carve_img<uint8_t>(base, off, w, h);
+            p.depn[l] = carve_img<float>(base, off, w, h);
         }
         p.vz = carve_img<float>(base, off, p.w, p.h);
+        p.vzn = carve_img<float>(base, off, p.w, p.h);
         off = round_up(off, 256);
         p.ws.icp_part = (float *)(base + off);
         off += round_up(sizeof(float) * 32 * maxb, 256);
@@ -236,7 +241,8 @@ int ensure_layout(odo_batch_t *b, const odo_pair *pairs, int n) {
 }
 
 // Writes every per-pair argument block into the pinned argument arena.
-void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float icpWeight, int fastOdom, int so3) {
+void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float icpWeight, int fastOdom, int so3,
+                int live_maps) {
     unsigned char *H = b->args_host;
     auto at = [&](size_t o) { return H + o; };
     const int icp = !rgbOnly && icpWeight > 0;
@@ -271,18 +277,43 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
         m.vz = p.vz.data;
         m.vz_pitch = p.vz.pitch;
         std::memcpy(at(b->o_model) + i * sizeof(ModelArgs), &m, sizeof(m));
+        // live maps (initICP(verts, norms)): planar pyramid, no transform,
+        // raw vertex z for the live photometric depth
+        if (live_maps) {
+            ModelArgs lm{};
+            lm.v4 = q.live_verts;
+            lm.n4 = q.live_norms;
+            lm.pitch4 = q.live_pitch;
+            lm.cols0 = p.w;
+            lm.rows0 = p.h;
+            for (int l = 0; l < kLevels; ++l) {
+                lm.vmap[l] = p.vc[l];
+                lm.nmap[l] = p.nc[l];
+            }
+            lm.do_transform = 0;
+            lm.vz = p.vzn.data;
+            lm.vz_pitch = p.vzn.pitch;
+            std::memcpy(at(b->o_live) + i * sizeof(ModelArgs), &lm, sizeof(lm));
+        }
+        // photometric depth of the live frame: the model's (depth input, the
+        // reference's quirk) or the live maps' own
+        Img<float> *depn = live_maps ? p.depn : p.dep;
         // photometric level 0: model image + depth from the model vertices,
         // live image, previous live image (SO3)
         const uint8_t *src[3] = {q.model_rgba, q.rgba, q.prev_rgba ? q.prev_rgba : q.rgba};
         const size_t sp[3] = {q.model_rgba_pitch, q.rgba_pitch, q.prev_rgba ? q.prev_rgba_pitch : q.rgba_pitch};
         Img<uint8_t> *imgs[3] = {p.last, p.next, p.lastnext};
         for (int r = 0; r < 3; ++r) {
-            RgbdArgs a{p.vz.data, p.vz.pitch, src[r], sp[r], p.dep[0], imgs[r][0], r == 0 ? 1 : 0};
+            // depth rows: the model's (role 0) and, for live maps, the live one (role 1)
+            const int with_depth = r == 0 || (r == 1 && live_maps);
+            Img<float> *dp = r == 1 ? depn : p.dep;
+            const Img<float> &vzr = r == 1 ? p.vzn : p.vz;
+            RgbdArgs a{vzr.data, vzr.pitch, src[r], sp[r], dp[0], imgs[r][0], with_depth};
             std::memcpy(at(b->o_rgbd[r]) + i * sizeof(RgbdArgs), &a, sizeof(a));
             for (int l = 0; l < 2; ++l) {
-                Img<const float> ds{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
+                Img<const float> ds{dp[l].data, dp[l].pitch, dp[l].cols, dp[l].rows};
                 Img<const uint8_t> is{imgs[r][l].data, imgs[r][l].pitch, imgs[r][l].cols, imgs[r][l].rows};
-                GaussArgs g{ds, p.dep[l + 1], is, imgs[r][l + 1], r == 0 ? 1 : 0};
+                GaussArgs g{ds, dp[l + 1], is, imgs[r][l + 1], with_depth};
                 std::memcpy(at(b->o_gauss[r][l]) + i * sizeof(GaussArgs), &g, sizeof(g));
             }
         }
@@ -316,7 +347,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             d.src[l] = Img<const uint8_t>{p.next[l].data, p.next[l].pitch, p.next[l].cols, p.next[l].rows};
             d.dx[l] = p.dx[l];
             d.dy[l] = p.dy[l];
-            d.depth[l] = Img<const float>{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
+            d.depth[l] = Img<const float>{depn[l].data, depn[l].pitch, depn[l].cols, depn[l].rows};
             d.cand[l] = p.cand[l];
             d.minScale[l] = (float)(pow(minGrad[l], 2.0) / pow((double)sobelScale, 2.0));
         }
@@ -344,7 +375,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
             L.dIdx = Img<const int16_t>{p.dx[l].data, p.dx[l].pitch, p.dx[l].cols, p.dx[l].rows};
             L.dIdy = Img<const int16_t>{p.dy[l].data, p.dy[l].pitch, p.dy[l].cols, p.dy[l].rows};
             L.lastDepth = Img<const float>{p.dep[l].data, p.dep[l].pitch, p.dep[l].cols, p.dep[l].rows};
-            L.nextDepth = L.lastDepth;
+            L.nextDepth = Img<const float>{depn[l].data, depn[l].pitch, depn[l].cols, depn[l].rows};
             L.lastImage = Img<const uint8_t>{p.last[l].data, p.last[l].pitch, p.last[l].cols, p.last[l].rows};
             L.nextImage = Img<const uint8_t>{p.next[l].data, p.next[l].pitch, p.next[l].cols, p.next[l].rows};
             L.corr = p.corr[l];
@@ -394,7 +425,7 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
 // the pairs' buffers (a fall-back call right after the warm-started call on
 // the same slots) except the extra intensity pyramid the SO3 stage reads.
 cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, const int max_iters[kLevels],
-                          bool prep = true) {
+                          bool prep = true, int live_maps = 0) {
     cudaStream_t s = b->stream;
     cudaError_t e = cudaMemcpyAsync(b->args_dev, b->args_host, b->args_bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
@@ -402,15 +433,17 @@ cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, con
     const int W = b->max_w, Hh = b->max_h;
     if (e == cudaSuccess) e = launch_stamp_batch(b->st_dev, n, s);
     if (e == cudaSuccess && prep) e = launch_model_maps_batch((const ModelArgs *)A(b->o_model), n, W, Hh, s);
+    if (e == cudaSuccess && prep && live_maps)
+        e = launch_model_maps_batch((const ModelArgs *)A(b->o_live), n, W, Hh, s);
     const int roles = so3 ? 3 : 2, r0 = prep ? 0 : 2;
     for (int r = r0; r < roles && e == cudaSuccess; ++r)
         e = launch_rgbd_level0_batch((const RgbdArgs *)A(b->o_rgbd[r]), n, W, Hh, s);
     for (int l = 0; l < 2 && e == cudaSuccess; ++l)
         for (int r = r0; r < roles && e == cudaSuccess; ++r)
             e = launch_gauss_down_batch((const GaussArgs *)A(b->o_gauss[r][l]), n, W >> (l + 1), Hh >> (l + 1), s);
-    for (int l = 0; l < 2 && e == cudaSuccess && prep; ++l)
+    for (int l = 0; l < 2 && e == cudaSuccess && prep && !live_maps; ++l)
         e = launch_pyr_down_depth_batch((const PyrArgs *)A(b->o_pyr[l]), n, W >> (l + 1), Hh >> (l + 1), s);
-    if (e == cudaSuccess && prep) e = launch_vmap_nmap_batch((const VNArgs *)A(b->o_vn), n, W, Hh, s);
+    if (e == cudaSuccess && prep && !live_maps) e = launch_vmap_nmap_batch((const VNArgs *)A(b->o_vn), n, W, Hh, s);
     if (e == cudaSuccess && rgb && prep)
         e = launch_derivatives_batch((const DerivArgs *)A(b->o_deriv), n, W, Hh, s);
     if (e == cudaSuccess && so3) e = launch_so3_batch((const So3Args *)A(b->o_so3), n, s);
@@ -456,6 +489,7 @@ int odo_batch_create(int max_pairs, odo_batch_t **out) {
     };
     const size_t np = (size_t)max_pairs;
     b->o_model = take(np * sizeof(ModelArgs));
+    b->o_live = take(np * sizeof(ModelArgs));
     for (int r = 0; r < 3; ++r) b->o_rgbd[r] = take(np * sizeof(RgbdArgs));
     for (int r = 0; r < 3; ++r)
         for (int l = 0; l < 2; ++l) b->o_gauss[r][l] = take(np * sizeof(GaussArgs));
@@ -535,14 +569,23 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
                int fastOdom, int so3, odo_pair_result *results, bool graph = true,
                const int *reuse_slots = nullptr) {
     if (!b || !pairs || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
+    const int live_maps = pairs[0].live_verts != nullptr;
     for (int i = 0; i < npairs; ++i) {
         const odo_pair &q = pairs[i];
         if (q.width < 16 || q.height < 16 || q.width > 8192 || q.height > 8192 || q.levels < 1 || q.levels > 3 ||
-            !q.model_verts || !q.model_norms || !q.model_rgba || !q.depth || !q.rgba ||
-            q.model_pitch < (size_t)q.width * 16 || q.depth_pitch < (size_t)q.width * 2 ||
-            q.rgba_pitch < (size_t)q.width * 4 || q.model_rgba_pitch < (size_t)q.width * 4 || !(q.fx != 0) ||
-            !(q.fy != 0))
+            !q.model_verts || !q.model_norms || !q.model_rgba || !q.rgba ||
+            q.model_pitch < (size_t)q.width * 16 || q.rgba_pitch < (size_t)q.width * 4 ||
+            q.model_rgba_pitch < (size_t)q.width * 4 || !(q.fx != 0) || !(q.fy != 0) ||
+            (q.model_pitch % 16) != 0 || ((uintptr_t)q.model_verts % 16) != 0 || ((uintptr_t)q.model_norms % 16) != 0)
             return ODO_ERR_ARG;
+        if ((q.live_verts != nullptr) != (live_maps != 0)) return ODO_ERR_ARG;  // one kind of live input per call
+        if (live_maps) {
+            if (!q.live_norms || q.live_pitch < (size_t)q.width * 16 || (q.live_pitch % 16) != 0 ||
+                ((uintptr_t)q.live_verts % 16) != 0 || ((uintptr_t)q.live_norms % 16) != 0)
+                return ODO_ERR_ARG;
+        } else if (!q.depth || q.depth_pitch < (size_t)q.width * 2) {
+            return ODO_ERR_ARG;
+        }
         for (int l = 0; l < kLevels; ++l)
             if (q.iterations[l] < 0 || q.iterations[l] > 20) return ODO_ERR_ARG;
     }
@@ -562,7 +605,7 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
     else rc = ensure_layout(b, pairs, npairs);
     if (rc != ODO_OK) return rc;
     const int rgb = rgbOnly || icpWeight < 100;
-    build_args(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3);
+    build_args(b, pairs, npairs, rgbOnly, icpWeight, fastOdom, so3, live_maps);
     int max_iters[kLevels] = {0, 0, 0};
     const int base[kLevels] = {fastOdom ? 3 : 10, 5, 4};
     for (int i = 0; i < npairs; ++i)
@@ -573,15 +616,15 @@ int track_impl(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *i
     if (warm && init != b->init_dev)
         BCK(cudaMemcpyAsync(b->init_dev, init, sizeof(float) * 6 * npairs, cudaMemcpyDeviceToDevice, b->stream));
     if (!graph) {
-        BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters, !reuse));
+        BCK(enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters, !reuse, live_maps));
     } else {
         GKey key{npairs, rgb, so3 ? 1 : 0, warm, max_iters[0], max_iters[1], max_iters[2], b->threads, b->ppt,
-                 b->split_solve};
+                 b->split_solve, live_maps};
         auto it = b->graphs.find(key);
         if (it == b->graphs.end()) {
             cudaGraph_t g = nullptr;
             BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters);
+            cudaError_t e = enqueue_batch(b, npairs, rgb, so3 ? 1 : 0, warm, max_iters, true, live_maps);
             cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
             if (e != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
@@ -631,6 +674,29 @@ extern "C" {
 int odo_batch_track(odo_batch_t *b, const odo_pair *pairs, int npairs, int rgbOnly, float icpWeight, int fastOdom,
                     int so3, odo_pair_result *results) {
     return track_impl(b, pairs, npairs, nullptr, rgbOnly, icpWeight, fastOdom, so3, results);
+}
+
+int odo_batch_verify(odo_batch_t *b, const odo_pair *pairs, int npairs, const odo_verify_params *vp,
+                     odo_pair_result *results, double *covariance, int *accept) {
+    if (!vp || !accept) return ODO_ERR_ARG;
+    const int rc = track_impl(b, pairs, npairs, nullptr, vp->rgbOnly, vp->icpWeight, vp->fastOdom, vp->so3, results);
+    if (rc != ODO_OK) return rc;
+    for (int i = 0; i < npairs; ++i) {
+        const odo_pair_result &r = results[i];
+        // getCovariance: lastA.cast<double>().lu().inverse() (src/odom/RGBDOdometryef.cpp:597-600)
+        double cov[36];
+        se3::inverse6(r.lastA, cov);
+        if (covariance) std::memcpy(covariance + 36 * (size_t)i, cov, sizeof(cov));
+        bool ok = true;
+        // src/apps/elastic_fusion_file.cpp:479-488: covar(i, i) > covThresh rejects
+        if (vp->max_covariance > 0)
+            for (int k = 0; k < 6; ++k) ok = ok && !(cov[k * 7] > vp->max_covariance);
+        // src/lc/Ferns.cpp:279, src/apps/elastic_fusion_file.cpp:498
+        if (vp->min_icp_count > 0) ok = ok && r.lastICPCount > vp->min_icp_count;
+        if (vp->max_icp_error > 0) ok = ok && r.lastICPError < vp->max_icp_error;
+        accept[i] = ok ? 1 : 0;
+    }
+    return ODO_OK;
 }
 
 int odo_batch_track_init(odo_batch_t *b, const odo_pair *pairs, int npairs, const float *init_dev, int rgbOnly,
