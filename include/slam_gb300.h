@@ -86,6 +86,26 @@ int odo_set_stream(odo_t *h, void *stream);
 /* initICP(GPUTexture* filteredDepth, depthCutoff), src/odom/RGBDOdometryef.cpp:118-142 */
 int odo_init_icp_depth(odo_t *h, const uint16_t *depth, size_t pitch_bytes, float depthCutoff);
 
+/* The reference's depth pre-filter followed by initICP(depth): the FILTER
+ * compute pack (src/gl/shaders/depth_bilateral.frag:30-76, a 13x13 bilateral
+ * filter of the raw depth that zeroes values outside [300 mm, maxD]) feeding
+ * initICP(DEPTH_FILTERED) (src/apps/elastic_fusion_file.cpp:349-370).  The
+ * filtered image goes straight into the handle's level-0 depth. */
+int odo_init_icp_raw_depth(odo_t *h, const uint16_t *raw_depth, size_t pitch_bytes, float maxD, float depthCutoff);
+
+/* The depth pre-filter alone, device to device on `stream` (NULL: legacy
+ * default stream); no handle:
+ *  odo_filter_depth  depth_bilateral.frag (src/gl/shaders/depth_bilateral.frag:30-76),
+ *                    u16 mm -> u16 mm;
+ *  odo_depth_metric  depth_metric.frag (src/gl/shaders/depth_metric.frag:28-40),
+ *                    u16 mm -> float m, 0 outside [300 mm, maxD].
+ * maxD in metres (the reference's maxDepthProcessed / depthCutoff); out must
+ * not overlap raw. */
+int odo_filter_depth(const uint16_t *raw, size_t raw_pitch, uint16_t *out, size_t out_pitch, int width, int height,
+                     float maxD, void *stream);
+int odo_depth_metric(const uint16_t *raw, size_t raw_pitch, float *out, size_t out_pitch, int width, int height,
+                     float maxD, void *stream);
+
 /* initICP(GPUTexture* verts, GPUTexture* norms, depthCutoff), src/odom/RGBDOdometryef.cpp:144-167 */
 int odo_init_icp_maps(odo_t *h, const float *verts, const float *norms, size_t pitch_bytes, float depthCutoff);
 

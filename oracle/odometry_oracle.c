@@ -159,6 +159,62 @@ void orc_derivatives(const uint8_t *src, int w, int h, int16_t *dx, int16_t *dy,
         }
 }
 
+/* uint(maxD * 1000.0f) of the depth shaders */
+static unsigned depth_max_mm(float maxD) {
+    float m = maxD * 1000.0f;
+    return m <= 0.f ? 0u : (m >= 4294967040.f ? 0xffffffffu : (unsigned)m);
+}
+
+/* depth_bilateral.frag, src/gl/shaders/depth_bilateral.frag:30-76 (a GL
+ * fragment shader in the reference): for a raw depth value in
+ * [300, uint(maxD * 1000)], round(sum1 / sum2) over the 13x13 window clipped
+ * to the image, taps row by row, w = exp(-(space2 * 0.024691358 + color2 *
+ * 0.000555556)); other pixels 0.  The neighbours are read at their own texel
+ * (the shader samples the texel corner cx / cols, which selects texel cx).
+ * Rounding to nearest, ties to even; tie[] flags quotients within 2e-3 of a
+ * half-integer, where another exp implementation may round the other way. */
+void orc_depth_bilateral(const uint16_t *raw, int w, int h, float maxD, uint16_t *out, uint8_t *tie) {
+    const unsigned max_mm = depth_max_mm(maxD);
+    const float ks = 0.024691358f, kc = 0.000555556f;
+    #pragma omp parallel for schedule(static)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const unsigned value = raw[(size_t)y * w + x];
+            uint16_t o = 0;
+            uint8_t t = 0;
+            if (!(value > max_mm || value < 300u)) {
+                const float v = (float)value;
+                const int tx = x - 6 + 13 < w ? x - 6 + 13 : w;
+                const int ty = y - 6 + 13 < h ? y - 6 + 13 : h;
+                float sum1 = 0.f, sum2 = 0.f;
+                for (int cy = y - 6 > 0 ? y - 6 : 0; cy < ty; ++cy)
+                    for (int cx = x - 6 > 0 ? x - 6 : 0; cx < tx; ++cx) {
+                        const float tmp = (float)raw[(size_t)cy * w + cx];
+                        const float dx = (float)x - (float)cx, dy = (float)y - (float)cy;
+                        const float space2 = dx * dx + dy * dy;
+                        const float dc = v - tmp;
+                        const float color2 = dc * dc;
+                        const float weight = expf(-(space2 * ks + color2 * kc));
+                        sum1 += tmp * weight;
+                        sum2 += weight;
+                    }
+                const float q = sum1 / sum2;
+                o = (uint16_t)nearbyintf(q);
+                t = fabsf(fabsf(q - floorf(q)) - 0.5f) < 2e-3f;
+            }
+            out[(size_t)y * w + x] = o;
+            if (tie) tie[(size_t)y * w + x] = t;
+        }
+}
+
+/* depth_metric.frag, src/gl/shaders/depth_metric.frag:28-40: metres, 0
+ * outside [300, uint(maxD * 1000)]. */
+void orc_depth_metric(const uint16_t *raw, int w, int h, float maxD, float *out) {
+    const unsigned max_mm = depth_max_mm(maxD);
+    for (size_t i = 0; i < (size_t)w * h; ++i)
+        out[i] = (raw[i] > max_mm || raw[i] < 300u) ? 0.f : (float)raw[i] / 1000.0f;
+}
+
 /* thread control for the timed CPU baseline */
 void orc_set_threads(int n) {
 #ifdef _OPENMP

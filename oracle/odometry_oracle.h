@@ -46,6 +46,10 @@ void orc_pyr_down_depth(const uint16_t *src, int sw, int sh, uint16_t *dst);
 void orc_bgr_to_intensity(const uint8_t *rgba, int w, int h, uint8_t *dst, uint8_t *tie);
 void orc_pyr_down_uchar_gauss(const uint8_t *src, int sw, int sh, uint8_t *dst, uint8_t *tie);
 void orc_derivatives(const uint8_t *src, int w, int h, int16_t *dx, int16_t *dy, uint8_t *tie);
+/* depth pre-filter shaders of the reference (src/gl/shaders/depth_bilateral.frag,
+ * depth_metric.frag) */
+void orc_depth_bilateral(const uint16_t *raw, int w, int h, float maxD, uint16_t *out, uint8_t *tie);
+void orc_depth_metric(const uint16_t *raw, int w, int h, float maxD, float *out);
 
 #ifdef __cplusplus
 }

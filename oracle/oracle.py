@@ -79,6 +79,26 @@ def pyr_down_uchar_gauss(src, with_tie=False):
     return (dst, tie) if with_tie else dst
 
 
+def depth_bilateral(raw, maxD, with_tie=False):
+    """depth_bilateral.frag (src/gl/shaders/depth_bilateral.frag:30-76) on a
+    raw u16 depth image; (filtered, tie flags) when with_tie."""
+    raw = np.ascontiguousarray(raw, np.uint16)
+    h, w = raw.shape
+    out = np.zeros((h, w), np.uint16)
+    tie = np.zeros((h, w), np.uint8)
+    lib().orc_depth_bilateral(_p(raw), w, h, ctypes.c_float(maxD), _p(out), _p(tie))
+    return (out, tie) if with_tie else out
+
+
+def depth_metric(raw, maxD):
+    """depth_metric.frag (src/gl/shaders/depth_metric.frag:28-40): metres."""
+    raw = np.ascontiguousarray(raw, np.uint16)
+    h, w = raw.shape
+    out = np.zeros((h, w), np.float32)
+    lib().orc_depth_metric(_p(raw), w, h, ctypes.c_float(maxD), _p(out))
+    return out
+
+
 def derivatives(src, with_tie=False):
     h, w = src.shape
     src = np.ascontiguousarray(src, dtype=np.uint8)

@@ -93,6 +93,9 @@ SIGNATURES = [
     ("odo_set_stream", c_int, [c_void_p, c_void_p]),
     ("odo_init_icp_depth", c_int, [c_void_p, c_void_p, c_size_t, c_float]),
     ("odo_init_icp_maps", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float]),
+    ("odo_init_icp_raw_depth", c_int, [c_void_p, c_void_p, c_size_t, c_float, c_float]),
+    ("odo_filter_depth", c_int, [c_void_p, c_size_t, c_void_p, c_size_t, c_int, c_int, c_float, c_void_p]),
+    ("odo_depth_metric", c_int, [c_void_p, c_size_t, c_void_p, c_size_t, c_int, c_int, c_float, c_void_p]),
     ("odo_init_icp_model", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float, P(c_float)]),
     ("odo_init_rgb", c_int, [c_void_p, c_void_p, c_size_t]),
     ("odo_init_rgb_model", c_int, [c_void_p, c_void_p, c_size_t]),

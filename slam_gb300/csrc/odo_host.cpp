@@ -409,12 +409,10 @@ int odo_set_precision(odo_t *h, int precision) {
     return ODO_OK;
 }
 
-int odo_init_icp_depth(odo_t *h, const uint16_t *depth, size_t pitch_bytes, float depthCutoff) {
-    if (!h || !depth || pitch_bytes < (size_t)h->width * 2) return ODO_ERR_ARG;
-    CK(follow_caller(h));
+// Level-0 depth in depth_tmp[0] (copied or filtered there): the pyramid and
+// the vertex / normal maps of every level (src/odom/RGBDOdometryef.cpp:131-139).
+static int icp_depth_from_level0(odo_t *h, float depthCutoff) {
     cudaStream_t s = h->stream;
-    CK(cudaMemcpy2DAsync(h->depth_tmp[0].data, h->depth_tmp[0].pitch, depth, pitch_bytes, (size_t)h->width * 2,
-                         h->height, cudaMemcpyDeviceToDevice, s));
     for (int l = 1; l < kLevels; ++l)
         CK(launch_pyr_down_depth(h->depth_tmp[l - 1].cimg(), h->depth_tmp[l].img(), s));
     Img<const uint16_t> d[kLevels];
@@ -428,6 +426,24 @@ int odo_init_icp_depth(odo_t *h, const uint16_t *depth, size_t pitch_bytes, floa
     }
     CK(launch_vmap_nmap(d, v, n, K, depthCutoff, kLevels, s));
     return ODO_OK;
+}
+
+int odo_init_icp_depth(odo_t *h, const uint16_t *depth, size_t pitch_bytes, float depthCutoff) {
+    if (!h || !depth || pitch_bytes < (size_t)h->width * 2) return ODO_ERR_ARG;
+    CK(follow_caller(h));
+    CK(cudaMemcpy2DAsync(h->depth_tmp[0].data, h->depth_tmp[0].pitch, depth, pitch_bytes, (size_t)h->width * 2,
+                         h->height, cudaMemcpyDeviceToDevice, h->stream));
+    return icp_depth_from_level0(h, depthCutoff);
+}
+
+int odo_init_icp_raw_depth(odo_t *h, const uint16_t *raw_depth, size_t pitch_bytes, float maxD, float depthCutoff) {
+    if (!h || !raw_depth || pitch_bytes < (size_t)h->width * 2 || (pitch_bytes % 2) || ((uintptr_t)raw_depth % 2) ||
+        !(maxD == maxD))
+        return ODO_ERR_ARG;
+    CK(follow_caller(h));
+    CK(launch_depth_bilateral(raw_depth, pitch_bytes, h->depth_tmp[0].data, h->depth_tmp[0].pitch, h->width,
+                              h->height, maxD, h->stream));
+    return icp_depth_from_level0(h, depthCutoff);
 }
 
 static int init_maps(odo_t *h, const float *verts, const float *norms, size_t pitch_bytes, const float *pose,

@@ -218,6 +218,10 @@ cudaError_t launch_track_begin(TrackState *st, cudaStream_t s);
 cudaError_t launch_so3(TrackState *st, Img<const uint8_t> last, Img<const uint8_t> next, Intr K2, cudaStream_t s);
 cudaError_t launch_level_iteration(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg, int iter,
                                    cudaStream_t s);
+// depth pre-filter (depth_filter.cu)
+cudaError_t launch_depth_bilateral(const uint16_t *src, size_t sp, uint16_t *dst, size_t dp, int cols, int rows,
+                                   float maxD, cudaStream_t s);
+
 // grid barriers of the persistent kernel give up after this many polls
 constexpr long long kPersistentSpinLimit = 1ll << 26;
 cudaError_t launch_level_persistent(const LevelArgs &L, TrackState *st, ReduceWs ws, const TrackLaunch &cfg,

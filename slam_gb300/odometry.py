@@ -114,6 +114,14 @@ class RGBDOdometry:
             self._check(self._L.odo_init_icp_maps(self._h, a.data_ptr(), b.data_ptr(), pitch, float(depthCutoff)),
                         "initICP")
 
+    def initICPRawDepth(self, raw_depth, maxD, depthCutoff=20.0):
+        """The reference's depth pre-filter (depth_bilateral.frag) on raw u16
+        depth, then initICP on the filtered image."""
+        import torch
+        pitch = _check_cuda_tensor(raw_depth, torch.uint16, (), "raw_depth")
+        self._check(self._L.odo_init_icp_raw_depth(self._h, raw_depth.data_ptr(), pitch, float(maxD),
+                                                   float(depthCutoff)), "initICPRawDepth")
+
     def initICPModel(self, verts, norms, depthCutoff, modelPose):
         import torch
         pitch = _check_cuda_tensor(verts, torch.float32, (4,), "verts")
@@ -264,3 +272,36 @@ class RGBDOdometry:
 
     def debug_derivatives(self):
         self._check(self._L.odo_debug_derivatives(self._h), "debug_derivatives")
+
+
+def filter_depth(raw, maxD, out=None):
+    """depth_bilateral.frag (src/gl/shaders/depth_bilateral.frag:30-76) on the
+    GPU: raw u16 depth (mm, CUDA tensor [h][w]) -> filtered u16 depth, on the
+    current torch stream."""
+    import torch
+    L = _native.load()
+    pitch = _check_cuda_tensor(raw, torch.uint16, (), "raw")
+    h, w = raw.shape
+    out = torch.empty((h, w), dtype=torch.uint16, device=raw.device) if out is None else out
+    opitch = _check_cuda_tensor(out, torch.uint16, (), "out")
+    rc = L.odo_filter_depth(raw.data_ptr(), pitch, out.data_ptr(), opitch, w, h, float(maxD),
+                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise OdometryError(rc, "odo_filter_depth failed")
+    return out
+
+
+def depth_metric(raw, maxD, out=None):
+    """depth_metric.frag (src/gl/shaders/depth_metric.frag:28-40) on the GPU:
+    raw u16 depth (mm) -> float metres, 0 outside [300 mm, maxD]."""
+    import torch
+    L = _native.load()
+    pitch = _check_cuda_tensor(raw, torch.uint16, (), "raw")
+    h, w = raw.shape
+    out = torch.empty((h, w), dtype=torch.float32, device=raw.device) if out is None else out
+    opitch = _check_cuda_tensor(out, torch.float32, (), "out")
+    rc = L.odo_depth_metric(raw.data_ptr(), pitch, out.data_ptr(), opitch, w, h, float(maxD),
+                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise OdometryError(rc, "odo_depth_metric failed")
+    return out
