@@ -106,6 +106,42 @@ int odo_filter_depth(const uint16_t *raw, size_t raw_pitch, uint16_t *out, size_
 int odo_depth_metric(const uint16_t *raw, size_t raw_pitch, float *out, size_t out_pitch, int width, int height,
                      float maxD, void *stream);
 
+/* ---- model prediction and fill-in (the producers of initICPModel's maps) ----
+ * IndexMap::combinedPredict (src/model/IndexMap.cpp:243-345, shaders
+ * src/model/shaders/splat.vert + combo_splat.frag) as CUDA splatting of the
+ * surfel map: surfels [n][12] float (device, 16-byte aligned): position xyz +
+ * confidence, colour (packed rgb as float) + unused + init time + last
+ * update time, normal xyz + radius -- the reference's Vertex layout
+ * (3 x vec4).  t_inv = the inverse of the camera pose (row-major 4x4; only
+ * its first three rows are read).  Outputs (device, any may be NULL): RGBA
+ * image (4 B/px), vertex and normal maps (RGBA32F, camera frame; all zero
+ * where nothing was drawn) and the u16 time map.  scratch: device memory of
+ * odo_model_predict_scratch_bytes(width, height) bytes, 8-byte aligned (the
+ * depth-test buffer).  Asynchronous on `stream`. */
+typedef struct {
+    int width, height;
+    float cx, cy, fx, fy;
+    float maxDepth;       /* depthCutoff */
+    float confThreshold;
+    int time, maxTime, timeDelta;
+} odo_predict_params;
+size_t odo_model_predict_scratch_bytes(int width, int height);
+int odo_model_predict(const float *surfels, int nsurfels, const float t_inv[16], const odo_predict_params *p,
+                      void *scratch, uint8_t *image, size_t image_pitch, float *vertex, float *normal,
+                      size_t map_pitch, uint16_t *time, size_t time_pitch, void *stream);
+/* FillIn::vertex / normal / image (src/gl/FillIn.cpp, shaders
+ * src/gl/shaders/fill_vertex.frag, fill_normal.frag, fill_rgb.frag): the
+ * predicted maps with their holes (vertex or normal z == 0, rgb sum 0) -- or
+ * everything when passthrough != 0 -- filled from the raw frame: vertices
+ * from the filtered u16 depth (mm), normals from forward differences of
+ * those vertices, colour from raw_rgba.  Outputs may be NULL (that fill is
+ * skipped); asynchronous on `stream`. */
+int odo_fill_in(const float *pred_vertex, const float *pred_normal, size_t pred_map_pitch, const uint8_t *pred_image,
+                size_t pred_image_pitch, const uint16_t *raw_depth, size_t raw_depth_pitch, const uint8_t *raw_rgba,
+                size_t raw_rgba_pitch, int width, int height, float cx, float cy, float fx, float fy,
+                int passthrough, float *out_vertex, float *out_normal, size_t out_map_pitch, uint8_t *out_image,
+                size_t out_image_pitch, void *stream);
+
 /* initICP(GPUTexture* verts, GPUTexture* norms, depthCutoff), src/odom/RGBDOdometryef.cpp:144-167 */
 int odo_init_icp_maps(odo_t *h, const float *verts, const float *norms, size_t pitch_bytes, float depthCutoff);
 

@@ -215,6 +215,180 @@ void orc_depth_metric(const uint16_t *raw, int w, int h, float maxD, float *out)
         out[i] = (raw[i] > max_mm || raw[i] < 300u) ? 0.f : (float)raw[i] / 1000.0f;
 }
 
+/* ---- model prediction (src/model/shaders/splat.vert, combo_splat.frag) and
+ * fill-in (src/gl/shaders/fill_vertex.frag, fill_normal.frag, fill_rgb.frag),
+ * single-operation rounded FP32 in the shaders' order, IEEE division and
+ * square root; the depth test keeps the nearest fragment, the lower surfel
+ * index on equal depth. */
+typedef struct { float px, py, pz, conf, nx, ny, nz, rad, xw, yw, size; } orc_splat;
+
+static void norm3f(float *x, float *y, float *z) {
+    float l = sqrtf(*x * *x + *y * *y + *z * *z);
+    *x = *x / l; *y = *y / l; *z = *z / l;
+}
+
+/* splat.vert, src/model/shaders/splat.vert:45-80 */
+static int splat_vertex(const float *t, const float *S, float cx, float cy, float fx, float fy, int cols, int rows,
+                        float maxDepth, float confThreshold, int time, int maxTime, int timeDelta, orc_splat *s) {
+    const float *P = S, *C = S + 4, *N = S + 8;
+    float hx = t[0] * P[0] + t[1] * P[1] + t[2] * P[2] + t[3];
+    float hy = t[4] * P[0] + t[5] * P[1] + t[6] * P[2] + t[7];
+    float hz = t[8] * P[0] + t[9] * P[1] + t[10] * P[2] + t[11];
+    if (hz > maxDepth || hz < 0.f || P[3] < confThreshold || (float)time - C[3] > (float)timeDelta ||
+        C[3] > (float)maxTime)
+        return 0;
+    s->px = hx; s->py = hy; s->pz = hz; s->conf = P[3];
+    float nx = t[0] * N[0] + t[1] * N[1] + t[2] * N[2];
+    float ny = t[4] * N[0] + t[5] * N[1] + t[6] * N[2];
+    float nz = t[8] * N[0] + t[9] * N[1] + t[10] * N[2];
+    norm3f(&nx, &ny, &nz);
+    s->nx = nx; s->ny = ny; s->nz = nz; s->rad = N[3];
+    float hc = (float)cols * 0.5f, hr = (float)rows * 0.5f;
+    float ndx = ((fx * hx) / hz + cx - hc) / hc, ndy = ((fy * hy) / hz + cy - hr) / hr;
+    s->xw = (ndx + 1.f) * hc;
+    s->yw = (ndy + 1.f) * hr;
+    float ax = ny - nz, ay = -nx, az = nx;
+    norm3f(&ax, &ay, &az);
+    ax = ax * N[3] * 1.41421356f; ay = ay * N[3] * 1.41421356f; az = az * N[3] * 1.41421356f;
+    float bx = ny * az - nz * ay, by = nz * ax - nx * az, bz = nx * ay - ny * ax;
+    float ox[4] = {ax, bx, -bx, -ax}, oy[4] = {ay, by, -by, -ay}, oz[4] = {az, bz, -bz, -az};
+    float xmin = 3.4e38f, xmax = -3.4e38f, ymin = 3.4e38f, ymax = -3.4e38f;
+    for (int q = 0; q < 4; ++q) {
+        float qx = hx + ox[q], qy = hy + oy[q], qz = hz + oz[q];
+        float u = (fx * qx) / qz + cx, v = (fy * qy) / qz + cy;
+        xmin = fminf(xmin, u); xmax = fmaxf(xmax, u); ymin = fminf(ymin, v); ymax = fmaxf(ymax, v);
+    }
+    float size = fmaxf(0.f, fmaxf(fabsf(xmax - xmin), fabsf(ymax - ymin)));
+    s->size = fminf(fmaxf(size, 1.f), 2047.f);
+    (void)rows;
+    return 1;
+}
+
+/* combo_splat.frag, src/model/shaders/combo_splat.frag:35-58 */
+static int splat_fragment(const orc_splat *s, int x, int y, float cx, float cy, float fx, float fy, float *z) {
+    float u = (float)x + 0.5f, v = (float)y + 0.5f;
+    float lx = (u - cx) / fx, ly = (v - cy) / fy, lz = 1.f;
+    norm3f(&lx, &ly, &lz);
+    float f = (s->px * s->nx + s->py * s->ny + s->pz * s->nz) / (lx * s->nx + ly * s->ny + lz * s->nz);
+    float qx = f * lx, qy = f * ly, qz = f * lz;
+    float dx = qx - s->px, dy = qy - s->py, dz = qz - s->pz;
+    if (dx * dx + dy * dy + dz * dz > s->rad * s->rad) return 0;
+    *z = qz;
+    return 1;
+}
+
+/* IndexMap::combinedPredict, src/model/IndexMap.cpp:243-345.  surfels [n][12];
+ * outputs image [h][w][4] u8, vertex / normal [h][w][4] f32, time [h][w] u16. */
+void orc_model_predict(const float *surfels, int n, const float *t_inv, int cols, int rows, float cx, float cy,
+                       float fx, float fy, float maxDepth, float confThreshold, int time, int maxTime, int timeDelta,
+                       uint8_t *image, float *vertex, float *normal, uint16_t *tmap) {
+    const size_t np = (size_t)cols * rows;
+    uint64_t *z = (uint64_t *)malloc(np * sizeof(uint64_t));
+    for (size_t i = 0; i < np; ++i) z[i] = ~0ull;
+    for (int i = 0; i < n; ++i) {
+        orc_splat s;
+        if (!splat_vertex(t_inv, surfels + 12 * (size_t)i, cx, cy, fx, fy, cols, rows, maxDepth, confThreshold, time,
+                          maxTime, timeDelta, &s))
+            continue;
+        if (!isfinite(s.xw) || !isfinite(s.yw)) continue;
+        float h = s.size * 0.5f;
+        float lo_x = s.xw - h - 0.5f, hi_x = s.xw + h - 0.5f, lo_y = s.yw - h - 0.5f, hi_y = s.yw + h - 0.5f;
+        int x0 = (int)ceilf(fmaxf(lo_x, 0.f)), y0 = (int)ceilf(fmaxf(lo_y, 0.f));
+        int x1 = (int)ceilf(fminf(hi_x, (float)cols)) - 1, y1 = (int)ceilf(fminf(hi_y, (float)rows)) - 1;
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                float zz;
+                if (!splat_fragment(&s, x, y, cx, cy, fx, fy, &zz)) continue;
+                float depth = zz / (2.f * maxDepth) + 0.5f;
+                depth = fminf(fmaxf(depth, 0.f), 1.f);
+                if (!(depth < 1.f)) continue;
+                uint32_t db;
+                memcpy(&db, &depth, 4);
+                uint64_t key = ((uint64_t)db << 32) | (uint32_t)i;
+                if (key < z[(size_t)y * cols + x]) z[(size_t)y * cols + x] = key;
+            }
+    }
+    const float ifx = 1.f / fx, ify = 1.f / fy;
+    for (int y = 0; y < rows; ++y)
+        for (int x = 0; x < cols; ++x) {
+            size_t p = (size_t)y * cols + x;
+            uint8_t im[4] = {0, 0, 0, 0};
+            float vo[4] = {0, 0, 0, 0}, no[4] = {0, 0, 0, 0};
+            uint16_t tm = 0;
+            if (z[p] != ~0ull) {
+                const float *S = surfels + 12 * (size_t)(uint32_t)(z[p] & 0xffffffffu);
+                orc_splat s;
+                float zz = 0.f;
+                splat_vertex(t_inv, S, cx, cy, fx, fy, cols, rows, maxDepth, confThreshold, time, maxTime, timeDelta,
+                             &s);
+                splat_fragment(&s, x, y, cx, cy, fx, fy, &zz);
+                int c = (int)S[4];
+                im[0] = (uint8_t)((c >> 16) & 0xff); im[1] = (uint8_t)((c >> 8) & 0xff); im[2] = (uint8_t)(c & 0xff);
+                im[3] = 255;
+                vo[0] = ((float)x + 0.5f - cx) * zz * ifx; vo[1] = ((float)y + 0.5f - cy) * zz * ify;
+                vo[2] = zz; vo[3] = s.conf;
+                no[0] = s.nx; no[1] = s.ny; no[2] = s.nz; no[3] = s.rad;
+                float tf = S[6];
+                tm = tf <= 0.f ? 0 : (tf >= 65535.f ? 65535 : (uint16_t)tf);
+            }
+            if (image) memcpy(image + 4 * p, im, 4);
+            if (vertex) memcpy(vertex + 4 * p, vo, 16);
+            if (normal) memcpy(normal + 4 * p, no, 16);
+            if (tmap) tmap[p] = tm;
+        }
+    free(z);
+}
+
+/* getVertex of src/gl/shaders/geometry.glsl:48-53 on u16 mm depth, edge-clamped */
+static void fill_raw_vertex(const uint16_t *d, int cols, int rows, float cx, float cy, float ifx, float ify, int x,
+                            int y, float *v) {
+    x = x < 0 ? 0 : (x >= cols ? cols - 1 : x);
+    y = y < 0 ? 0 : (y >= rows ? rows - 1 : y);
+    float z = (float)d[(size_t)y * cols + x] / 1000.0f;
+    v[0] = ((float)x - cx) * z * ifx; v[1] = ((float)y - cy) * z * ify; v[2] = z;
+}
+
+/* FillIn::vertex / normal / image (fill_vertex.frag:37-53, fill_normal.frag:34-50,
+ * fill_rgb.frag:29-37); dense images, outputs may be NULL. */
+void orc_fill_in(const float *pv, const float *pn, const uint8_t *pi, const uint16_t *raw_d, const uint8_t *raw_rgba,
+                 int cols, int rows, float cx, float cy, float fx, float fy, int passthrough, float *ov, float *on,
+                 uint8_t *oi) {
+    const float ifx = 1.f / fx, ify = 1.f / fy;
+    for (int y = 0; y < rows; ++y)
+        for (int x = 0; x < cols; ++x) {
+            size_t p = (size_t)y * cols + x;
+            if (ov) {
+                memcpy(ov + 4 * p, pv + 4 * p, 16);
+                if (pv[4 * p + 2] == 0.f || passthrough) {
+                    float v[3];
+                    fill_raw_vertex(raw_d, cols, rows, cx, cy, ifx, ify, x, y, v);
+                    ov[4 * p] = v[0]; ov[4 * p + 1] = v[1]; ov[4 * p + 2] = v[2]; ov[4 * p + 3] = 1.f;
+                }
+            }
+            if (on) {
+                memcpy(on + 4 * p, pn + 4 * p, 16);
+                if (pn[4 * p + 2] == 0.f || passthrough) {
+                    float v[3], vx[3], vy[3];
+                    fill_raw_vertex(raw_d, cols, rows, cx, cy, ifx, ify, x, y, v);
+                    fill_raw_vertex(raw_d, cols, rows, cx, cy, ifx, ify, x + 1, y, vx);
+                    fill_raw_vertex(raw_d, cols, rows, cx, cy, ifx, ify, x, y + 1, vy);
+                    float ax = vx[0] - v[0], ay = vx[1] - v[1], az = vx[2] - v[2];
+                    float bx = vy[0] - v[0], by = vy[1] - v[1], bz = vy[2] - v[2];
+                    float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
+                    norm3f(&nx, &ny, &nz);
+                    on[4 * p] = nx; on[4 * p + 1] = ny; on[4 * p + 2] = nz; on[4 * p + 3] = 1.f;
+                }
+            }
+            if (oi) {
+                memcpy(oi + 4 * p, pi + 4 * p, 4);
+                if ((int)pi[4 * p] + pi[4 * p + 1] + pi[4 * p + 2] == 0 || passthrough) {
+                    memcpy(oi + 4 * p, raw_rgba + 4 * p, 3);
+                    oi[4 * p + 3] = 255;
+                }
+            }
+        }
+}
+
 /* thread control for the timed CPU baseline */
 void orc_set_threads(int n) {
 #ifdef _OPENMP

@@ -50,6 +50,14 @@ void orc_derivatives(const uint8_t *src, int w, int h, int16_t *dx, int16_t *dy,
  * depth_metric.frag) */
 void orc_depth_bilateral(const uint16_t *raw, int w, int h, float maxD, uint16_t *out, uint8_t *tie);
 void orc_depth_metric(const uint16_t *raw, int w, int h, float maxD, float *out);
+/* model prediction and fill-in (src/model/shaders/splat.vert + combo_splat.frag,
+ * src/gl/shaders/fill_*.frag) */
+void orc_model_predict(const float *surfels, int n, const float *t_inv, int cols, int rows, float cx, float cy,
+                       float fx, float fy, float maxDepth, float confThreshold, int time, int maxTime, int timeDelta,
+                       uint8_t *image, float *vertex, float *normal, uint16_t *tmap);
+void orc_fill_in(const float *pv, const float *pn, const uint8_t *pi, const uint16_t *raw_d, const uint8_t *raw_rgba,
+                 int cols, int rows, float cx, float cy, float fx, float fy, int passthrough, float *ov, float *on,
+                 uint8_t *oi);
 
 #ifdef __cplusplus
 }

@@ -99,6 +99,36 @@ def depth_metric(raw, maxD):
     return out
 
 
+def model_predict(surfels, t_inv, cam, max_depth=20.0, conf_threshold=10.0, time=1, max_time=2 ** 30,
+                  time_delta=2 ** 30):
+    """IndexMap::combinedPredict (src/model/shaders/splat.vert, combo_splat.frag)
+    on the CPU: (image u8 [h,w,4], vertex f32 [h,w,4], normal f32 [h,w,4], time u16 [h,w])."""
+    s = np.ascontiguousarray(surfels, np.float32)
+    t = np.ascontiguousarray(np.asarray(t_inv, np.float32).reshape(16))
+    w, h = cam.width, cam.height
+    image = np.zeros((h, w, 4), np.uint8)
+    vertex = np.zeros((h, w, 4), np.float32)
+    normal = np.zeros((h, w, 4), np.float32)
+    tm = np.zeros((h, w), np.uint16)
+    f = ctypes.c_float
+    lib().orc_model_predict(_p(s), len(s), _p(t), w, h, f(cam.cx), f(cam.cy), f(cam.fx), f(cam.fy), f(max_depth),
+                            f(conf_threshold), int(time), int(max_time), int(time_delta), _p(image), _p(vertex),
+                            _p(normal), _p(tm))
+    return image, vertex, normal, tm
+
+
+def fill_in(pv, pn, pi, raw_depth, raw_rgba, cam, passthrough=False):
+    """FillIn::vertex / normal / image (src/gl/shaders/fill_*.frag) on the CPU."""
+    pv, pn = np.ascontiguousarray(pv, np.float32), np.ascontiguousarray(pn, np.float32)
+    pi, rd = np.ascontiguousarray(pi, np.uint8), np.ascontiguousarray(raw_depth, np.uint16)
+    rr = np.ascontiguousarray(raw_rgba, np.uint8)
+    ov, on, oi = np.zeros_like(pv), np.zeros_like(pn), np.zeros_like(pi)
+    f = ctypes.c_float
+    lib().orc_fill_in(_p(pv), _p(pn), _p(pi), _p(rd), _p(rr), cam.width, cam.height, f(cam.cx), f(cam.cy),
+                      f(cam.fx), f(cam.fy), int(bool(passthrough)), _p(ov), _p(on), _p(oi))
+    return ov, on, oi
+
+
 def derivatives(src, with_tie=False):
     h, w = src.shape
     src = np.ascontiguousarray(src, dtype=np.uint8)

@@ -76,6 +76,12 @@ class OdoPairResult(ctypes.Structure):
                 ("lastA", c_double * 36), ("lastb", c_double * 6)]
 
 
+class OdoPredictParams(ctypes.Structure):
+    _fields_ = [("width", c_int), ("height", c_int), ("cx", c_float), ("cy", c_float), ("fx", c_float),
+                ("fy", c_float), ("maxDepth", c_float), ("confThreshold", c_float), ("time", c_int),
+                ("maxTime", c_int), ("timeDelta", c_int)]
+
+
 class OdoVerifyParams(ctypes.Structure):
     _fields_ = [("rgbOnly", c_int), ("icpWeight", c_float), ("fastOdom", c_int), ("so3", c_int),
                 ("max_icp_error", c_float), ("min_icp_count", c_float), ("max_covariance", c_double)]
@@ -94,6 +100,12 @@ SIGNATURES = [
     ("odo_init_icp_depth", c_int, [c_void_p, c_void_p, c_size_t, c_float]),
     ("odo_init_icp_maps", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float]),
     ("odo_init_icp_raw_depth", c_int, [c_void_p, c_void_p, c_size_t, c_float, c_float]),
+    ("odo_model_predict_scratch_bytes", c_size_t, [c_int, c_int]),
+    ("odo_model_predict", c_int, [c_void_p, c_int, P(c_float), P(OdoPredictParams), c_void_p, c_void_p, c_size_t,
+                                  c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
+    ("odo_fill_in", c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_size_t,
+                            c_int, c_int, c_float, c_float, c_float, c_float, c_int, c_void_p, c_void_p, c_size_t,
+                            c_void_p, c_size_t, c_void_p]),
     ("odo_filter_depth", c_int, [c_void_p, c_size_t, c_void_p, c_size_t, c_int, c_int, c_float, c_void_p]),
     ("odo_depth_metric", c_int, [c_void_p, c_size_t, c_void_p, c_size_t, c_int, c_int, c_float, c_void_p]),
     ("odo_init_icp_model", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float, P(c_float)]),
