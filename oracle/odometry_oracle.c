@@ -483,8 +483,16 @@ static inline int near_thr(double a, double t, double rel) {
  * the other way.  The pose difference between a normal and a flipped run
  * measures how much the tracking result depends on decisions the reference's
  * approximate division may take differently from IEEE arithmetic. */
-static int g_flip_ties = 0;
+static int g_flip_ties = 0;  /* 0 none, 1 all ties, 2 / 3 the two halves of a hash of the tied value */
 void ORC(set_flip_ties)(int on) { g_flip_ties = on; }
+
+static inline int flip_this(double v) {
+    if (g_flip_ties == 1) return 1;
+    uint64_t b;
+    memcpy(&b, &v, sizeof(b));
+    b ^= b >> 33; b *= 0xff51afd7ed558ccdull; b ^= b >> 33;
+    return (int)(b & 1) == g_flip_ties - 2;
+}
 
 /* __float2int_rn of a quotient, flagging (and, when flipping, reversing) a
  * rounding that sits on a tie. */
@@ -492,7 +500,7 @@ static inline int round_q(real q, int *tie) {
     int r = f2i_rn(q);
     if (near_half(q, TIE_REL, fabs((double)q) + 1.0)) {
         *tie = 1;
-        if (g_flip_ties) {
+        if (g_flip_ties && flip_this((double)q)) {
             const double fl = floor((double)q);
             r = (r == (int)fl) ? (int)fl + 1 : (int)fl;
         }
@@ -503,7 +511,7 @@ static inline int round_q(real q, int *tie) {
 static inline int decide(int result, double a, double t, int *tie) {
     if (near_thr(a, t, TIE_REL)) {
         *tie = 1;
-        if (g_flip_ties) return !result;
+        if (g_flip_ties && flip_this(a)) return !result;
     }
     return result;
 }
@@ -1175,6 +1183,12 @@ typedef struct {
     /* keep_deriv != 0: the tracking call uses the derivative images already
      * in dIdx/dIdy (set through odo_buffer) instead of computing them */
     int keep_deriv;
+    /* the loop's discrete decisions (SO3 convergence / divergence tests, the
+     * rgbOnly early exit), numbered in the order taken: the smallest relative
+     * margin between the compared values and its index, and the index of a
+     * decision to take the other way (-1: none) */
+    int ndec, flip_decision, min_margin_index;
+    double min_margin;
     int nhist;
     double hist[32][9];
 } orc_odo;
@@ -1190,6 +1204,7 @@ static void intr_level(const orc_odo *o, int l, float *fx, float *fy, float *cx,
 orc_odo *ORC(odo_create)(int width, int height, float cx, float cy, float fx, float fy, float distThresh,
                          float angleThresh) {
     orc_odo *o = (orc_odo *)calloc(1, sizeof(orc_odo));
+    o->flip_decision = -1;
     o->width = width; o->height = height;
     o->cx = cx; o->cy = cy; o->fx = fx; o->fy = fy;
     o->distThres = distThresh; o->angleThres = angleThresh;
@@ -1304,12 +1319,25 @@ static void unpack29(const double *h, real *A, real *b) {
         }
 }
 
+/* One loop decision `result` from comparing a with b: records its margin,
+ * and reverses it when it is the decision chosen to be flipped. */
+static int loop_decision(orc_odo *o, int result, double a, double b) {
+    const double s = fabs(a) > fabs(b) ? fabs(a) : fabs(b);
+    const double m = s > 0 ? fabs(a - b) / s : 0.0;
+    const int k = o->ndec++;
+    if (m < o->min_margin) { o->min_margin = m; o->min_margin_index = k; }
+    return k == o->flip_decision ? !result : result;
+}
+
 /* getIncrementalTransformation, src/odom/RGBDOdometryef.cpp:267-595.
  * trans/rot: in = previous pose, out = new pose (rot row-major). */
 void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float icpWeight, int pyramid,
                     int fastOdom, int so3) {
     const int icp = !rgbOnly && icpWeight > 0;
     const int rgb = rgbOnly || icpWeight < 100;
+    o->ndec = 0;
+    o->min_margin = HUGE_VAL;
+    o->min_margin_index = -1;
     real Rprev[9], tprev[3], Rcurr[9], tcurr[3];
     memcpy(Rprev, rot, sizeof(Rprev)); memcpy(tprev, trans, sizeof(tprev));
     memcpy(Rcurr, Rprev, sizeof(Rcurr)); memcpy(tcurr, tprev, sizeof(tcurr));
@@ -1354,8 +1382,10 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
             }
             o->st.lastSO3Error = (float)(SQRT(res[0]) / res[1]);
             o->st.lastSO3Count = (float)res[1];
-            if (o->st.lastSO3Error < lastError && lastCount == o->st.lastSO3Count) break;
-            else if ((double)o->st.lastSO3Error > (double)lastError + 0.001) {
+            const int lower = loop_decision(o, o->st.lastSO3Error < lastError, o->st.lastSO3Error, lastError);
+            if (lower && lastCount == o->st.lastSO3Count) break;
+            else if (loop_decision(o, (double)o->st.lastSO3Error > (double)lastError + 0.001,
+                                   (double)o->st.lastSO3Error, (double)lastError + 0.001)) {
                 o->st.lastSO3Error = lastError; o->st.lastSO3Count = lastCount;
                 memcpy(resultR, lastResultR, sizeof(resultR));
                 break;
@@ -1435,7 +1465,7 @@ void ORC(odo_track)(orc_odo *o, real trans[3], real rot[9], int rgbOnly, float i
             /* src/odom/RGBDOdometryef.cpp:457-458, operator precedence kept */
             float sigmaVal = (float)sqrt((double)(((float)sigma / rgbSize == 0) ? 1 : rgbSize));
             float rgbError = (float)(sqrt((double)sigma) / (rgbSize == 0 ? 1 : rgbSize));
-            if (rgbOnly && rgbError > o->st.lastRGBError) break;
+            if (rgbOnly && loop_decision(o, rgbError > o->st.lastRGBError, rgbError, o->st.lastRGBError)) break;
             o->st.lastRGBError = rgbError;
             o->st.lastRGBCount = (float)rgbSize;
             if (rgbOnly) sigmaVal = -1;
@@ -1533,6 +1563,13 @@ void ORC(odo_set_schedule)(orc_odo *o, int levels, const int iters[3]) {
 }
 
 void ORC(odo_set_keep_derivatives)(orc_odo *o, int keep) { o->keep_deriv = keep; }
+void ORC(odo_set_flip_decision)(orc_odo *o, int index) { o->flip_decision = index; }
+/* smallest relative margin of the last tracking call's loop decisions, and
+ * its index (-1: no decision was taken) */
+double ORC(odo_decision_margin)(orc_odo *o, int *index) {
+    *index = o->min_margin_index;
+    return o->min_margin;
+}
 
 /* getCovariance, src/odom/RGBDOdometryef.cpp:597-600 */
 void ORC(odo_covariance)(orc_odo *o, double out[36]) { ORC(inverse6)(o->lastA, out); }

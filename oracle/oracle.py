@@ -267,10 +267,11 @@ class Kernels:
         return out
 
 
-def set_flip_ties(prec, on):
-    """Decisions flagged as rounding ties are taken the other way (the
-    per-pixel kernels and the tracking loop of the given precision)."""
-    Kernels(prec).f("set_flip_ties")(int(bool(on)))
+def set_flip_ties(prec, mode):
+    """Decisions flagged as rounding ties are taken the other way in the
+    per-pixel kernels of the given precision: mode 0 none, 1 all, 2 / 3 the
+    two halves of a hash of the tied value."""
+    Kernels(prec).f("set_flip_ties")(int(mode))
 
 
 def set_reverse_sums(prec, on):
@@ -396,6 +397,21 @@ class Odometry:
         a = np.ascontiguousarray(np.asarray(arr).astype(cur.dtype, copy=False).reshape(cur.shape))
         ptr = self.k.f("odo_buffer")(self._h, self.BUF[name], level)
         ctypes.memmove(ptr, a.ctypes.data, a.nbytes)
+
+    def set_flip_decision(self, index):
+        """The tracking loop takes its decision number `index` (SO3
+        convergence / divergence tests, the rgbOnly early exit, in the order
+        taken) the other way; -1: none."""
+        self.k.f("odo_set_flip_decision")(self._h, int(index))
+
+    def decision_margin(self):
+        """(smallest relative margin of the last call's loop decisions, its
+        index or -1)."""
+        f = self.k.f("odo_decision_margin")
+        f.restype = ctypes.c_double
+        idx = ctypes.c_int()
+        m = f(self._h, ctypes.byref(idx))
+        return m, idx.value
 
     def keep_derivatives(self, keep=True):
         """Tracking calls use the derivative images set with set_buffer

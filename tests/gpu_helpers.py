@@ -125,26 +125,33 @@ def set_images(o, images):
     o.keep_derivatives(True)
 
 
-# The oracle's own result is perturbed three ways to measure how precisely
-# the reference algorithm determines the pose on an input: its FP64 twin
-# (precision), every flagged tie decision taken the other way (the decisions
-# the reference's approximate division may take differently), and every
+# How precisely the reference algorithm determines the pose on an input is
+# measured by perturbing the oracle's own run: its FP64 twin (precision);
+# flagged rounding ties decided the other way -- all of them, and each half of
+# them by a hash (the decisions the reference's approximate division may take
+# differently; the GPU's kernels take a subset of them differently); every
 # pairwise sum in reverse order (summation order, which differs between any
-# two reduction trees).  A GPU pose within 1e-5 of the oracle's passes; beyond
-# that it must be within twice the sum of the three differences, and those
-# must all be below GAP_LIMIT for the flat bound to apply.  Where one exceeds
-# UNDETERMINED (1 cm / 10 mrad) the algorithm does not determine the pose on
-# this input (e.g. ICP alone diverging from a large motion): the pose is only
-# required to be finite, and the case is reported.
+# two reduction trees); and, when a loop decision (the SO3 convergence and
+# divergence tests, the rgbOnly early exit) compared two values within
+# DECISION_MARGIN, that decision taken the other way.  A GPU pose within 1e-5
+# of the oracle's passes; beyond that it must be within twice the sum of the
+# precision, tie (largest of the three), order and decision differences, all
+# of which must be below GAP_LIMIT for the flat bound to apply.  Where one
+# exceeds UNDETERMINED (1 cm / 10 mrad) the algorithm does not determine the
+# pose on this input (e.g. ICP alone diverging from a large motion): the pose
+# is only required to be finite, and the case is reported.
 UNDETERMINED = 1e-2
+DECISION_MARGIN = 1e-3
+PERTURBATIONS = {"fp64": (64, None), "ties": (32, 1), "ties_a": (32, 2), "ties_b": (32, 3), "order": (32, "reverse"),
+                 "decision": (32, "decision")}
 
 
 class OracleRuns:
     """The oracle's host loop on one tracking input, run on demand: FP32 (the
-    comparison) and its three perturbations.  load(o) puts the inputs into a
-    fresh oracle handle (the call order of the caller); start = (t, R) the
-    start pose; levels / iterations the batched tracker's per-pair schedule
-    (0: the reference's)."""
+    comparison) and its perturbations.  load(o) puts the inputs into a fresh
+    oracle handle (the call order of the caller); start = (t, R) the start
+    pose; levels / iterations the batched tracker's per-pair schedule (0: the
+    reference's)."""
 
     def __init__(self, cam, load, start, flags, levels=0, iterations=(0, 0, 0)):
         self.cam, self.load, self.start, self.flags = cam, load, start, dict(flags)
@@ -152,8 +159,9 @@ class OracleRuns:
         self._runs = {}
 
     def run(self, prec=32, perturb=None):
-        """perturb: None, "flip" (ties the other way) or "reverse" (sums in
-        reverse order)."""
+        """perturb: None; 1 / 2 / 3 (ties the other way: all, half A, half B);
+        "reverse" (sums in reverse order); "decision" (the closest loop
+        decision of the unperturbed run the other way)."""
         key = (prec, perturb)
         if key not in self._runs:
             from oracle import oracle
@@ -161,13 +169,15 @@ class OracleRuns:
             if self.levels:
                 o.set_schedule(self.levels, self.iterations)
             self.load(o)
-            oracle.set_flip_ties(prec, perturb == "flip")
+            if perturb == "decision":
+                o.set_flip_decision(self.run(prec)[2].decision_margin()[1])
+            oracle.set_flip_ties(prec, perturb if isinstance(perturb, int) else 0)
             oracle.set_reverse_sums(prec, perturb == "reverse")
             try:
                 t, R = o.getIncrementalTransformation(np.float32(self.start[0]).astype(o.k.real),
                                                       np.float32(self.start[1]).astype(o.k.real), **self.flags)
             finally:
-                oracle.set_flip_ties(prec, False)
+                oracle.set_flip_ties(prec, 0)
                 oracle.set_reverse_sums(prec, False)
             self._runs[key] = (np.asarray(t, np.float64), np.asarray(R, np.float64), o)
         return self._runs[key]
@@ -176,12 +186,19 @@ class OracleRuns:
     def main(self):
         return self.run(32)
 
+    def near_decision(self):
+        m, idx = self.run(32)[2].decision_margin()
+        return idx >= 0 and m < DECISION_MARGIN
+
+    def _perturbed(self):
+        return [k for k in PERTURBATIONS if k != "decision" or self.near_decision()]
+
     def sensitivity(self):
         """{name: (rad, m)} differences of the perturbed runs from the FP32 run."""
         t32, R32, _ = self.run(32)
         out = {}
-        for name, key in (("fp64", (64, None)), ("ties", (32, "flip")), ("order", (32, "reverse"))):
-            t, R, _ = self.run(*key)
+        for name in self._perturbed():
+            t, R, _ = self.run(*PERTURBATIONS[name])
             out[name] = pose_diff(t32, R32, t, R)
         return out
 
@@ -198,8 +215,17 @@ class OracleRuns:
             return float("inf"), float("inf"), "undetermined (" + how + ")"
         if worst < GAP_LIMIT:
             return POSE_TOL_RAD, POSE_TOL_M, "flat (" + how + ")"
-        return (max(POSE_TOL_RAD, 2 * sum(v[0] for v in s.values())),
-                max(POSE_TOL_M, 2 * sum(v[1] for v in s.values())), "widened (" + how + ")")
+        tie = [max(s[k][i] for k in ("ties", "ties_a", "ties_b")) for i in (0, 1)]
+        tol = [2 * (s["fp64"][i] + tie[i] + s["order"][i] + (s["decision"][i] if "decision" in s else 0.0))
+               for i in (0, 1)]
+        return max(POSE_TOL_RAD, tol[0]), max(POSE_TOL_M, tol[1]), "widened (" + how + ")"
+
+    def iterations_ok(self, gpu_iterations):
+        """The GPU's iteration counts equal the oracle's or those of one of
+        its FP32 perturbations (a near-tie loop decision may stop a loop one
+        iteration earlier or later)."""
+        runs = [self.run(32)] + [self.run(*PERTURBATIONS[k]) for k in self._perturbed() if k != "fp64"]
+        return any(list(gpu_iterations) == r[2].iterations() for r in runs)
 
     def jtj_tolerance(self, flat):
         """Relative tolerance of lastA: 1e-3 (sums of ~1e4-1e5 FP32 products
@@ -208,8 +234,7 @@ class OracleRuns:
         if flat:
             return 1e-3
         A = self.run(32)[2].stats["lastA"]
-        d = max(np.abs(self.run(*key)[2].stats["lastA"] - A).max()
-                for key in ((64, None), (32, "flip"), (32, "reverse")))
+        d = max(np.abs(self.run(*PERTURBATIONS[k])[2].stats["lastA"] - A).max() for k in self._perturbed())
         return max(1e-3, 2 * d / max(np.abs(A).max(), 1e-30))
 
 

@@ -54,7 +54,7 @@ def check_against_oracle(pairs, res, flags, tag):
             continue
         flat += is_flat
         worst = (max(worst[0], rot), max(worst[1], tr))
-        assert list(res[i].iterations) == o.iterations(), (label, list(res[i].iterations), o.iterations())
+        assert ref.iterations_ok(res[i].iterations), (label, list(res[i].iterations), o.iterations())
         st = o.stats
         assert abs(res[i].lastICPCount - st["lastICPCount"]) <= 0.002 * max(1.0, st["lastICPCount"]), label
         assert abs(res[i].lastRGBCount - st["lastRGBCount"]) <= 0.002 * max(1.0, st["lastRGBCount"]), label

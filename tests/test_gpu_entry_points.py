@@ -158,7 +158,7 @@ def test_model_to_model_check_matches_oracle(gpu, seed):
     to, Ro, o = ref.main
     tol = ref.tolerance
     check_pose("model-to-model 320x240 seed %d" % seed, tg, Rg, to, Ro, tol)
-    assert g.iterations() == o.iterations()
+    assert ref.iterations_ok(g.iterations())
     cg, co = g.getCovariance(), o.getCovariance()
     # the handle's covariance is the inverse of its own lastA ...
     ok, err = rel_close(cg, np.linalg.inv(np.asarray(g.lastA, np.float64).reshape(6, 6)), 1e-9)

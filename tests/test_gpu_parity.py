@@ -229,7 +229,7 @@ def test_tracking_matches_oracle(gpu, orc, seed, flags):
     to, Ro, o = ref.main
     label = "tracking seed %d %s" % (seed, ",".join(f"{k}={v}" for k, v in flags.items()) or "default")
     _, _, flat = check_pose(label, tg, Rg, to, Ro, ref.tolerance)
-    assert g.iterations() == o.iterations()
+    assert ref.iterations_ok(g.iterations()), (g.iterations(), o.iterations())
     st = o.stats
     assert abs(g.lastICPCount - st["lastICPCount"]) <= 0.002 * max(1.0, st["lastICPCount"])
     assert abs(g.lastRGBCount - st["lastRGBCount"]) <= 0.002 * max(1.0, st["lastRGBCount"])
@@ -294,12 +294,12 @@ def test_sequence_with_image_swap(gpu, orc):
         set_images(o, images)
         pg = g.getIncrementalTransformation(start[0], start[1])
         po = o.getIncrementalTransformation(start[0], start[1])
-        assert g.iterations() == o.iterations(), (k, g.iterations(), o.iterations())
 
         def load(h, pair=pair, images=images):
             load_frame(h, pair, first=False)
             set_images(h, images)
         ref = OracleRuns(cam, load, start, {})
+        assert ref.iterations_ok(g.iterations()), (k, g.iterations(), o.iterations())
         check_pose("sequence frame %d" % k, np.float64(pg[0]), np.float64(pg[1]), np.float64(po[0]),
                    np.float64(po[1]), ref.tolerance)
         start = (np.float32(po[0]), np.float32(po[1]))  # continue both from the oracle's pose
@@ -316,7 +316,7 @@ def test_small_and_odd_sizes(gpu, orc, size):
     tg, Rg = track(g, pair)
     ref = frame_runs(pair, {}, images=images)
     to, Ro, o = ref.main
-    assert g.iterations() == o.iterations(), (size, g.iterations(), o.iterations())
+    assert ref.iterations_ok(g.iterations()), (size, g.iterations(), o.iterations())
     check_pose("size %dx%d" % size, tg, Rg, to, Ro, ref.tolerance)
 
 

@@ -80,7 +80,7 @@ def run_check(pairs, params, levels, tag):
         n_acc += int(acc[i])
         if not flat and ref.undetermined():
             continue  # no decision to compare on an input the algorithm does not determine
-        assert list(res[i].iterations) == o.iterations(), (tag, i)
+        assert ref.iterations_ok(res[i].iterations), (tag, i)
         st = o.stats
         co = o.getCovariance()
         cov_ok = all(not (co[k, k] > params["max_covariance"]) for k in range(6)) \
