@@ -298,6 +298,27 @@ def run_ours(args):
     errs = [synth.pose_error(synth.pose(np.float64(R), np.float64(t)), frames[k]["T2"])
             for k, (t, R) in enumerate(poses[:len(frames)])]
 
+    # ---- the same frames in the other execution modes (persistent: one
+    # cooperative kernel per pyramid level; stream: the graph's kernels
+    # launched one by one) ----
+    mode_fps = {}
+    for name, m in (("persistent", MODE_PERSISTENT), ("stream", MODE_STREAM)):
+        if name == args.mode:
+            continue
+        odo.set_mode(m)
+        for k in range(3):
+            step(dframes[k % len(dframes)])
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(n_single):
+            step(dframes[k % len(dframes)])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        mode_fps[name] = n_single / (e0.elapsed_time(e1) / 1000.0)
+    odo.set_mode({"graph": MODE_GRAPH, "stream": MODE_STREAM, "persistent": MODE_PERSISTENT}[args.mode])
+    for k in range(3):
+        step(dframes[k % len(dframes)])
+
     # ---- end to end: host inputs copied per step ------------------------
     hframes = [{k: (v.cpu().pin_memory() if isinstance(v, torch.Tensor) else v) for k, v in f.items()}
                for f in dframes[:8]]
@@ -371,6 +392,7 @@ def run_ours(args):
                  "pose_error_vs_gt": {"rot_rad_mean": float(np.mean(rot)), "trans_m_mean": float(np.mean(tr)),
                                       "rot_rad_max": float(np.max(rot)), "trans_m_max": float(np.max(tr))},
                  "iterations": iters, "clocks": clk, "iteration_ms_by_level": level_ms,
+                 "frames_per_s_other_modes": mode_fps,
                  "device_phases_us": phases, "gpu_launches": launches_per_frame * n_single}
     warm = measure_warm_batched(args, stream, local, world)
     verif = measure_batched_verification(args, stream, world) if args.verify_pairs > 0 else None

@@ -227,15 +227,31 @@ class OracleRuns:
         runs = [self.run(32)] + [self.run(*PERTURBATIONS[k]) for k in self._perturbed() if k != "fp64"]
         return any(list(gpu_iterations) == r[2].iterations() for r in runs)
 
+    def spread(self, metric):
+        """Twice the combined change of metric(oracle handle) (a scalar) under
+        the perturbations: precision + ties (largest of the three) + order +
+        decision, as the pose bound combines them."""
+        base = metric(self.run(32)[2])
+        d = {k: abs(metric(self.run(*PERTURBATIONS[k])[2]) - base) for k in self._perturbed()}
+        tie = max(d[k] for k in ("ties", "ties_a", "ties_b"))
+        return 2 * (d["fp64"] + tie + d["order"] + d.get("decision", 0.0))
+
     def jtj_tolerance(self, flat):
-        """Relative tolerance of lastA: 1e-3 (sums of ~1e4-1e5 FP32 products
-        in another order) where the pose is within the flat bound, else also
-        twice the largest change of lastA among the oracle's runs."""
+        """Relative tolerance of lastA (max-normalised): 1e-3 (sums of
+        ~1e4-1e5 FP32 products in another order) where the pose is within the
+        flat bound, else also the combined spread of lastA."""
         if flat:
             return 1e-3
         A = self.run(32)[2].stats["lastA"]
-        d = max(np.abs(self.run(*PERTURBATIONS[k])[2].stats["lastA"] - A).max() for k in self._perturbed())
-        return max(1e-3, 2 * d / max(np.abs(A).max(), 1e-30))
+        scale = max(np.abs(A).max(), 1e-30)
+        return max(1e-3, max(self.spread(lambda o, i=i: o.stats["lastA"].reshape(-1)[i]) for i in range(36)) / scale)
+
+    def count_tolerance(self, name, flat):
+        """Tolerance of a final inlier / correspondence count ("lastICPCount",
+        "lastRGBCount"): 0.2 % (per-pixel decisions on rounding ties) where the
+        pose is within the flat bound, else also its combined spread."""
+        base = max(1.0, self.run(32)[2].stats[name])
+        return 0.002 * base if flat else max(0.002 * base, self.spread(lambda o: o.stats[name]))
 
 
 def frame_runs(pair, flags, levels=0, iterations=(0, 0, 0), first=True, images=None):

@@ -56,8 +56,9 @@ def check_against_oracle(pairs, res, flags, tag):
         worst = (max(worst[0], rot), max(worst[1], tr))
         assert ref.iterations_ok(res[i].iterations), (label, list(res[i].iterations), o.iterations())
         st = o.stats
-        assert abs(res[i].lastICPCount - st["lastICPCount"]) <= 0.002 * max(1.0, st["lastICPCount"]), label
-        assert abs(res[i].lastRGBCount - st["lastRGBCount"]) <= 0.002 * max(1.0, st["lastRGBCount"]), label
+        for name in ("lastICPCount", "lastRGBCount"):
+            assert abs(getattr(res[i], name) - st[name]) <= ref.count_tolerance(name, is_flat), \
+                (label, name, getattr(res[i], name), st[name])
     report("%s: %d/%d pairs within the flat 1e-5 bound, %d undetermined by the reference algorithm, max pose "
            "diff of the others %.2e rad %.2e m" % (tag, flat, len(pairs), undetermined, worst[0], worst[1]))
 
