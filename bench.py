@@ -92,6 +92,9 @@ def parse():
     ap.add_argument("--verify-pairs", type=int, default=512,
                     help="pairs per launch of the batched-verification line (0: skip it)")
     ap.add_argument("--residual-ratio", type=float, default=6.0)
+    ap.add_argument("--front-end", type=int, default=1,
+                    help="also time the producers of the tracker's inputs (depth pre-filter, model prediction, "
+                         "fill-in) at 640x480")
     a = ap.parse_args()
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
@@ -396,6 +399,7 @@ def run_ours(args):
                  "device_phases_us": phases, "gpu_launches": launches_per_frame * n_single}
     warm = measure_warm_batched(args, stream, local, world)
     verif = measure_batched_verification(args, stream, world) if args.verify_pairs > 0 else None
+    front = measure_front_end(args, stream) if rank == 0 and args.front_end else None
     if rank == 0:
         W = warm
         out = {"metric": METRIC, "value": W["fps"], "unit": "frames/s", "n_gpus": world, "steps": W["steps"],
@@ -418,12 +422,107 @@ def run_ours(args):
                            "vs_plain_batched": W["fps"] / W["plain_batched"]["frames_per_s"],
                            "eval_thresholds_vs_plain_batched": W["eval_thresholds"]["speedup_vs_plain_batched"]},
                "eval_thresholds": W["eval_thresholds"], "accuracy": W["accuracy"],
-               "batched_verification": verif, "clocks": W["clocks"],
+               "batched_verification": verif, "front_end": front, "clocks": W["clocks"],
                "gpu_launches": W["gpu_launches"], "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return out
+
+
+def measure_front_end(args, stream, reps=20):
+    """The producers of the tracker's inputs at 640x480, one frame per launch
+    as the reference runs them: depth_bilateral.frag / depth_metric.frag,
+    IndexMap::combinedPredict (surfel splatting) and FillIn, each timed with
+    CUDA events per launch with L2 flushed (a 256 MB write) between launches,
+    against its algorithmic bytes; the oracle's CPU restatement of the same
+    kernel is timed beside it."""
+    import torch
+    from oracle import oracle
+    from slam_gb300 import model, odometry, synth
+    cam = synth.Camera()
+    rng = np.random.default_rng(args.seed + 77)
+    scene = synth.make_room(args.seed + 77)
+    T0 = synth.room_camera(rng)
+    views = []
+    for _ in range(6):
+        T = T0 @ synth.random_motion(rng, 15.0, 0.3)
+        m = synth.render(scene, T, cam, depth=False, rgba=True, model=True)
+        S = model.surfels_from_view(m["vert"], m["norm"], m["rgba"], T, cam)
+        S[:, 3] = rng.uniform(5.0, 20.0, size=len(S)).astype(np.float32)
+        views.append(S)
+    S = np.concatenate(views)
+    fr = synth.render(scene, T0, cam, depth=True, rgba=True, model=False)
+    raw = fr["depth"]                      # sensor-like noise and dropout from the renderer
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    d_raw = torch.from_numpy(raw.view(np.int16)).cuda().view(torch.uint16)
+    d_rgba = dev(fr["rgba"])
+    d_S = dev(S)
+    params = model.predict_params(cam, conf_threshold=10.0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    scratch = torch.empty(_native_load().odo_model_predict_scratch_bytes(cam.width, cam.height) // 8,
+                          dtype=torch.int64, device="cuda")
+    peak, peak_kind = measured_peaks()
+    npx = cam.width * cam.height
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        ts = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(reps):
+            flush.fill_(1)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    def cpu_timed(fn, budget_s=2.0):
+        n, t0 = 0, time.perf_counter()
+        while True:
+            fn()
+            n += 1
+            if time.perf_counter() - t0 > budget_s:
+                return (time.perf_counter() - t0) * 1e3 / n
+
+    out = {}
+    pred = model.predict(d_S, T0, params, scratch=scratch)
+    hp = [p.cpu().numpy() for p in pred[:3]]
+    rows = [
+        ("depth_bilateral", lambda: odometry.filter_depth(d_raw, 20.0), 4 * npx,
+         "2 B read + 2 B written per pixel (13x13 window from a shared-memory tile)",
+         lambda: oracle.depth_bilateral(raw, 20.0)),
+        ("depth_metric", lambda: odometry.depth_metric(d_raw, 20.0), 6 * npx, "2 B read + 4 B written per pixel",
+         lambda: oracle.depth_metric(raw, 20.0)),
+        ("model_predict", lambda: model.predict(d_S, T0, params, scratch=scratch), 48 * len(S) + (8 + 38) * npx,
+         "48 B per surfel read, 8 B per pixel depth-index word, 38 B per pixel of maps written",
+         lambda: oracle.model_predict(S, model.t_inv_of(T0), cam, max_depth=20.0, conf_threshold=10.0, time=1,
+                                      max_time=2 ** 30, time_delta=2 ** 30)),
+        ("fill_in", lambda: model.fill_in(pred[1], pred[2], pred[0], d_raw, d_rgba, cam), (42 + 36) * npx,
+         "42 B read (predicted maps, raw depth and colour) + 36 B written per pixel",
+         lambda: oracle.fill_in(hp[1], hp[2], hp[0], raw, fr["rgba"], cam)),
+    ]
+    for name, fn, alg, what, cpu_fn in rows:
+        ms = timed(fn)
+        gbs = alg / (ms * 1e-3) / 1e9
+        row = {"ms": ms, "alg_bytes": int(alg), "alg_bytes_def": what, "achieved_gbs": gbs,
+               "frac_of_peak": gbs / peak, "peak_kind": peak_kind}
+        if cpu_fn is not None:
+            try:
+                row["cpu_oracle_ms"] = cpu_timed(cpu_fn)
+            except Exception as exc:
+                row["cpu_oracle_ms"] = f"failed: {exc}"
+        out[name] = row
+    out["workload"] = (f"640x480, one frame per launch; surfel map of {len(S)} surfels from 6 views of one room; "
+                       "L2 flushed between launches")
+    return out
+
+
+def _native_load():
+    from slam_gb300 import _native
+    return _native.load()
 
 
 def profile_traffic(name):

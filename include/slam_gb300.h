@@ -479,6 +479,14 @@ typedef struct {
 int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, int npairs,
                          const odo_warm_params *wp, odo_pair_result *results, int *fallback);
 
+/* PNG scanline filter reconstruction (filter types 0-4 of the PNG format)
+ * for the TUM-format frame reader, whose reference reads its PNG images
+ * through OpenCV (src/inputs/FileReader.cpp:43-55): `filtered` holds
+ * `height` rows of 1 filter-type byte + row_bytes bytes (the inflated IDAT
+ * stream), `out` receives height x row_bytes bytes; bpp = bytes per pixel
+ * (1..8).  Host memory; ODO_ERR_ARG on an unknown filter type. */
+int odo_png_unfilter(const uint8_t *filtered, int height, size_t row_bytes, int bpp, uint8_t *out);
+
 /* GPU ray caster of the synthetic test scenes (scene struct of the synthetic
  * data generator, synth_scene): view i of scene view_scene[i] at
  * camera-to-world pose poses[16 i .. 16 i + 15] (row-major), depth noise

@@ -31,7 +31,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.pat
 
 # translation units of the tracker library
 CU_SOURCES = ["odo_maps.cu", "odo_track.cu", "depth_filter.cu", "model_predict.cu", "cnn.cu", "synth_gpu.cu"]
-CPP_SOURCES = ["odo_host.cpp", "batch_host.cpp", "cnn_host.cpp"]
+CPP_SOURCES = ["odo_host.cpp", "batch_host.cpp", "cnn_host.cpp", "inputs_host.cpp"]
 
 
 def _newer(target, deps):

@@ -125,25 +125,85 @@ def set_images(o, images):
     o.keep_derivatives(True)
 
 
+# Rounding ties.  The reference divides and takes square roots in their
+# approximate forms; the oracle evaluates them in IEEE arithmetic and flags
+# the integer roundings and threshold tests that sit within a few ulp of a
+# decision boundary.  Where the reference's kernels are available (the
+# cubin of oracle/build_ref.py), every FP32 oracle run decides those ties
+# with the reference's own arithmetic: the run logs the operands of each
+# tie, the reference's `a / b` and sqrtf are evaluated on them on the GPU
+# with the reference's flags (oracle/ref_shim.cu, shim_arith), and the run
+# is repeated with those results until it meets no new tie.  The oracle is
+# then an exact restatement of the reference's per-pixel arithmetic, on its
+# own trajectory.  _TIES caches the results (a pure function of the
+# operands) across runs.
+_TIES = {}
+_REF = []
+
+
+def _reference_kernels():
+    if not _REF:
+        try:
+            from oracle import ref_runner
+            _REF.append(ref_runner.RefKernels() if ref_runner.available() else None)
+        except Exception:
+            _REF.append(None)
+    return _REF[0]
+
+
+def ties_resolved():
+    return _reference_kernels() is not None
+
+
+def resolved(run_once, max_runs=8):
+    """run_once() (a fresh FP32 oracle run) with its ties decided by the
+    reference's arithmetic; without the reference's kernels, run_once()."""
+    from oracle import oracle
+    rk = _reference_kernels()
+    if rk is None:
+        return run_once()
+    oracle.set_resolve_ties(32, True)
+    try:
+        for _ in range(max_runs):
+            oracle.take_tie_log(32)
+            res = run_once()
+            new = {tuple(k) for k in oracle.take_tie_log(32).tolist()} - _TIES.keys()
+            if not new:
+                return res
+            keys = np.array(sorted(new), np.uint32)
+            _TIES.update(zip(map(tuple, keys.tolist()), rk.arith(keys).tolist()))
+            oracle.set_tie_table(32, np.array(list(_TIES.keys()), np.uint32),
+                                 np.array(list(_TIES.values()), np.uint32))
+        raise AssertionError("oracle run still meets new rounding ties after %d runs" % max_runs)
+    finally:
+        oracle.set_resolve_ties(32, False)
+
+
 # How precisely the reference algorithm determines the pose on an input is
 # measured by perturbing the oracle's own run: its FP64 twin (precision);
-# flagged rounding ties decided the other way -- all of them, and each half of
-# them by a hash (the decisions the reference's approximate division may take
-# differently; the GPU's kernels take a subset of them differently); every
-# pairwise sum in reverse order (summation order, which differs between any
-# two reduction trees); and, when a loop decision (the SO3 convergence and
-# divergence tests, the rgbOnly early exit) compared two values within
-# DECISION_MARGIN, that decision taken the other way.  A GPU pose within 1e-5
-# of the oracle's passes; beyond that it must be within twice the sum of the
-# precision, tie (largest of the three), order and decision differences, all
-# of which must be below GAP_LIMIT for the flat bound to apply.  Where one
+# two other summation orders of every pairwise sum (reversed; split at a
+# third) -- the GPU's reduction tree is another order again; and, when a
+# loop decision (the SO3 convergence and divergence tests, the rgbOnly early
+# exit) compared two values within DECISION_MARGIN, that decision taken the
+# other way.  Without the reference's kernels the ties themselves are free:
+# then flagged ties decided the other way -- all of them, and each half of
+# them by a hash -- are perturbations too.  A GPU pose within 1e-5 of the
+# oracle's passes; beyond that it must be within twice the sum of the
+# precision, tie (largest), order (largest) and decision differences, all of
+# which must be below GAP_LIMIT for the flat bound to apply.  Where one
 # exceeds UNDETERMINED (1 cm / 10 mrad) the algorithm does not determine the
 # pose on this input (e.g. ICP alone diverging from a large motion): the pose
 # is only required to be finite, and the case is reported.
 UNDETERMINED = 1e-2
 DECISION_MARGIN = 1e-3
-PERTURBATIONS = {"fp64": (64, None), "ties": (32, 1), "ties_a": (32, 2), "ties_b": (32, 3), "order": (32, "reverse"),
-                 "decision": (32, "decision")}
+PERTURBATIONS_RESOLVED = {"fp64": (64, None), "order": (32, "reverse"), "order_b": (32, "third"),
+                          "decision": (32, "decision")}
+PERTURBATIONS_IEEE = {"fp64": (64, None), "ties": (32, 1), "ties_a": (32, 2), "ties_b": (32, 3),
+                      "order": (32, "reverse"), "order_b": (32, "third"), "decision": (32, "decision")}
+
+
+def perturbations():
+    return PERTURBATIONS_RESOLVED if ties_resolved() else PERTURBATIONS_IEEE
 
 
 class OracleRuns:
@@ -160,26 +220,32 @@ class OracleRuns:
 
     def run(self, prec=32, perturb=None):
         """perturb: None; 1 / 2 / 3 (ties the other way: all, half A, half B);
-        "reverse" (sums in reverse order); "decision" (the closest loop
-        decision of the unperturbed run the other way)."""
+        "reverse" / "third" (other summation orders); "decision" (the closest
+        loop decision of the unperturbed run the other way).  FP32 runs decide
+        their ties with the reference's arithmetic where it is available."""
         key = (prec, perturb)
         if key not in self._runs:
             from oracle import oracle
-            o = new_oracle_odo(self.cam, prec)
-            if self.levels:
-                o.set_schedule(self.levels, self.iterations)
-            self.load(o)
-            if perturb == "decision":
-                o.set_flip_decision(self.run(prec)[2].decision_margin()[1])
-            oracle.set_flip_ties(prec, perturb if isinstance(perturb, int) else 0)
-            oracle.set_reverse_sums(prec, perturb == "reverse")
-            try:
-                t, R = o.getIncrementalTransformation(np.float32(self.start[0]).astype(o.k.real),
-                                                      np.float32(self.start[1]).astype(o.k.real), **self.flags)
-            finally:
-                oracle.set_flip_ties(prec, 0)
-                oracle.set_reverse_sums(prec, False)
-            self._runs[key] = (np.asarray(t, np.float64), np.asarray(R, np.float64), o)
+            flip_decision = self.run(prec)[2].decision_margin()[1] if perturb == "decision" else None
+
+            def once():
+                o = new_oracle_odo(self.cam, prec)
+                if self.levels:
+                    o.set_schedule(self.levels, self.iterations)
+                self.load(o)
+                if flip_decision is not None:
+                    o.set_flip_decision(flip_decision)
+                oracle.set_flip_ties(prec, perturb if isinstance(perturb, int) else 0)
+                oracle.set_reverse_sums(prec, {"reverse": 1, "third": 2}.get(perturb, 0))
+                try:
+                    t, R = o.getIncrementalTransformation(np.float32(self.start[0]).astype(o.k.real),
+                                                          np.float32(self.start[1]).astype(o.k.real), **self.flags)
+                finally:
+                    oracle.set_flip_ties(prec, 0)
+                    oracle.set_reverse_sums(prec, 0)
+                return np.asarray(t, np.float64), np.asarray(R, np.float64), o
+
+            self._runs[key] = resolved(once) if prec == 32 else once()
         return self._runs[key]
 
     @property
@@ -191,14 +257,14 @@ class OracleRuns:
         return idx >= 0 and m < DECISION_MARGIN
 
     def _perturbed(self):
-        return [k for k in PERTURBATIONS if k != "decision" or self.near_decision()]
+        return [k for k in perturbations() if k != "decision" or self.near_decision()]
 
     def sensitivity(self):
         """{name: (rad, m)} differences of the perturbed runs from the FP32 run."""
         t32, R32, _ = self.run(32)
         out = {}
         for name in self._perturbed():
-            t, R, _ = self.run(*PERTURBATIONS[name])
+            t, R, _ = self.run(*perturbations()[name])
             out[name] = pose_diff(t32, R32, t, R)
         return out
 
@@ -215,8 +281,9 @@ class OracleRuns:
             return float("inf"), float("inf"), "undetermined (" + how + ")"
         if worst < GAP_LIMIT:
             return POSE_TOL_RAD, POSE_TOL_M, "flat (" + how + ")"
-        tie = [max(s[k][i] for k in ("ties", "ties_a", "ties_b")) for i in (0, 1)]
-        tol = [2 * (s["fp64"][i] + tie[i] + s["order"][i] + (s["decision"][i] if "decision" in s else 0.0))
+        tie = [max([s[k][i] for k in ("ties", "ties_a", "ties_b") if k in s] + [0.0]) for i in (0, 1)]
+        order = [max(s["order"][i], s["order_b"][i]) for i in (0, 1)]
+        tol = [2 * (s["fp64"][i] + tie[i] + order[i] + (s["decision"][i] if "decision" in s else 0.0))
                for i in (0, 1)]
         return max(POSE_TOL_RAD, tol[0]), max(POSE_TOL_M, tol[1]), "widened (" + how + ")"
 
@@ -224,7 +291,7 @@ class OracleRuns:
         """The GPU's iteration counts equal the oracle's or those of one of
         its FP32 perturbations (a near-tie loop decision may stop a loop one
         iteration earlier or later)."""
-        runs = [self.run(32)] + [self.run(*PERTURBATIONS[k]) for k in self._perturbed() if k != "fp64"]
+        runs = [self.run(32)] + [self.run(*perturbations()[k]) for k in self._perturbed() if k != "fp64"]
         return any(list(gpu_iterations) == r[2].iterations() for r in runs)
 
     def spread(self, metric):
@@ -232,9 +299,9 @@ class OracleRuns:
         the perturbations: precision + ties (largest of the three) + order +
         decision, as the pose bound combines them."""
         base = metric(self.run(32)[2])
-        d = {k: abs(metric(self.run(*PERTURBATIONS[k])[2]) - base) for k in self._perturbed()}
-        tie = max(d[k] for k in ("ties", "ties_a", "ties_b"))
-        return 2 * (d["fp64"] + tie + d["order"] + d.get("decision", 0.0))
+        d = {k: abs(metric(self.run(*perturbations()[k])[2]) - base) for k in self._perturbed()}
+        tie = max([d[k] for k in ("ties", "ties_a", "ties_b") if k in d] + [0.0])
+        return 2 * (d["fp64"] + tie + max(d["order"], d["order_b"]) + d.get("decision", 0.0))
 
     def jtj_tolerance(self, flat):
         """Relative tolerance of lastA (max-normalised): 1e-3 (sums of

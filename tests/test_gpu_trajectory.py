@@ -4,14 +4,15 @@ smooth Catmull-Rom camera path at 30 fps (<= 1.5 deg / 3 cm per frame)
 through a seeded room; each frame's model prediction is ray-cast from the
 ground-truth scene at the current pose estimate, the live frame (noisy depth +
 RGB) at the true pose.  Every frame is tracked by the GPU handle and by the
-oracle's host loop from the same start pose, on handles that carry their
-state (the SO3 image swap) from frame to frame; per-frame pose and JtJ
-(lastA) are compared, and the max / p99 of both are reported."""
+oracle's host loop from the same start pose (the GPU handle carries its
+state -- the SO3 image swap -- from frame to frame; the oracle gets that
+state with the GPU's reference-exact images); per-frame pose and JtJ (lastA)
+are compared, and the max / p99 of both are reported."""
 import numpy as np
 import pytest
 
 from gpu_helpers import (POSE_TOL_M, POSE_TOL_RAD, OracleRuns, check_pose, dev, dev_u16, gpu_images, new_gpu_odo,
-                         new_oracle_odo, pose_diff, report, set_images)
+                         pose_diff, report, set_images)
 
 pytestmark = pytest.mark.gpu
 
@@ -25,10 +26,8 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
     scene = synth.make_room(seed)
     T = synth.trajectory(seed, FRAMES)
     g = new_gpu_odo(cam)
-    o = new_oracle_odo(cam)
     prev = synth.render(scene, T[0], cam, noise_seed=seed * 100003, depth=False, rgba=True)
     g.initFirstRGB(dev(prev["rgba"]))
-    o.initFirstRGB(prev["rgba"])
     est = [T[0].astype(np.float32).astype(np.float64)]
     rot_err, tr_err, jtj_err = [], [], []
     for k in range(1, FRAMES):
@@ -39,17 +38,9 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
         g.initRGBModel(dev(model["rgba"]))
         g.initICP(dev_u16(live["depth"]), 20.0)
         g.initRGB(dev(live["rgba"]))
-        o.initICPModel(model["vert"], model["norm"], 20.0, start)
-        o.initRGBModel(model["rgba"])
-        o.initICP(live["depth"], 20.0)
-        o.initRGB(live["rgba"])
         images = gpu_images(g)
-        set_images(o, images)
         tg, Rg = g.getIncrementalTransformation(start[:3, 3], start[:3, :3])
-        to, Ro = o.getIncrementalTransformation(start[:3, 3], start[:3, :3])
-        tg, Rg, to, Ro = (np.asarray(x, np.float64) for x in (tg, Rg, to, Ro))
-        rot, tr = pose_diff(tg, Rg, to, Ro)
-        flat = rot <= POSE_TOL_RAD and tr <= POSE_TOL_M
+        tg, Rg = np.asarray(tg, np.float64), np.asarray(Rg, np.float64)
 
         def load(h, model=model, live=live, start=start, images=images):
             # a fresh handle with the GPU's images (lastNextImage included)
@@ -60,6 +51,9 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
             h.initRGB(live["rgba"])
             set_images(h, images)
         ref = OracleRuns(cam, load, (start[:3, 3], start[:3, :3]), {})
+        to, Ro, o = ref.main
+        rot, tr = pose_diff(tg, Rg, to, Ro)
+        flat = rot <= POSE_TOL_RAD and tr <= POSE_TOL_M
         assert g.iterations() == o.iterations() or ref.iterations_ok(g.iterations()), \
             (k, g.iterations(), o.iterations())
         if not flat:
