@@ -1192,6 +1192,12 @@ def run_warm_study(args):
         e1.record(stream)
         torch.cuda.synchronize()
         t_warm += e0.elapsed_time(e1) / reps
+        if c == 0:
+            # one more step of each, bracketed by NVTX ranges, for a profiler's
+            # launch list (ncu --nvtx --nvtx-include "warm_step/" ...)
+            for name, fn in (("plain_step", lambda: b.track(fps, descs=descs)),
+                             ("warm_step", lambda: b.track_warm(net, fps, descs=descs, **wkw))):
+                _nvtx(name, fn)
         rows["plain"].append(_res_array(rp))
         rows["warm"].append(_res_array(rw))
         fbs.append(fb)
@@ -1266,6 +1272,24 @@ def run_warm_study(args):
            "fp64_oracle": {"pairs": len(orc), "plain_within_1e-5": within(0), "warm_within_1e-5": within(1),
                            "oracle_vs_gt_rot_p50": float(np.median([x[2][0] for x in orc])) if orc else None}}
     print(json.dumps(out), flush=True)
+
+
+def _nvtx(name, fn):
+    """fn() inside an NVTX push/pop range (when torch has NVTX)."""
+    import torch
+    torch.cuda.synchronize()
+    try:
+        torch.cuda.nvtx.range_push(name)
+        pushed = True
+    except Exception:
+        pushed = False
+    try:
+        out = fn()
+        torch.cuda.synchronize()
+    finally:
+        if pushed:
+            torch.cuda.nvtx.range_pop()
+    return out
 
 
 def main():

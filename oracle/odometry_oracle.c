@@ -483,89 +483,19 @@ static inline int near_thr(double a, double t, double rel) {
  * the other way.  The pose difference between a normal and a flipped run
  * measures how much the tracking result depends on decisions the reference's
  * approximate division may take differently from IEEE arithmetic. */
-static int g_flip_ties = 0;  /* 0 none, 1 all ties, 2 / 3 the two halves of a hash of the tied value */
+/* 0 none, 1 all ties, m >= 2: half (m - 2) % 2 of the ties by a hash of the
+ * tied value with seed (m - 2) / 2 (modes 2 and 3 are complementary halves,
+ * 4 and 5 another split, ...) */
+static int g_flip_ties = 0;
 void ORC(set_flip_ties)(int on) { g_flip_ties = on; }
 
 static inline int flip_this(double v) {
     if (g_flip_ties == 1) return 1;
     uint64_t b;
     memcpy(&b, &v, sizeof(b));
+    b ^= 0x9e3779b97f4a7c15ull * (uint64_t)((g_flip_ties - 2) / 2);
     b ^= b >> 33; b *= 0xff51afd7ed558ccdull; b ^= b >> 33;
-    return (int)(b & 1) == g_flip_ties - 2;
-}
-
-/* Tie resolution by the reference's own arithmetic (test infrastructure,
- * FP32 build only).  The reference divides and takes square roots in their
- * approximate forms (--prec-div=false --prec-sqrt=false,
- * src/CMakeLists.txt:116).  When resolution is on, a flagged tie looks its
- * operands up in a table of results of that arithmetic (filled by the
- * caller, which evaluates the reference's `a / b` and sqrtf on the GPU with
- * the reference's flags) and uses the recorded result; operands missing
- * from the table are logged for the caller and the IEEE result stands.
- * Keys: (kind, a, b, c) bit patterns; kind 0 = __float2int_rn(a / b + c),
- * kind 1 = sqrtf(a). */
-typedef struct { uint32_t k[4]; uint32_t v; } tie_entry;
-static tie_entry *g_tie_tab = NULL;
-static int g_tie_tab_n = 0;
-static uint32_t *g_tie_log = NULL;
-static int g_tie_log_n = 0, g_tie_log_cap = 0;
-static int g_resolve_ties = 0;
-static int tie_key_cmp(const void *a, const void *b) {
-    const uint32_t *x = (const uint32_t *)a, *y = (const uint32_t *)b;
-    for (int i = 0; i < 4; ++i)
-        if (x[i] != y[i]) return x[i] < y[i] ? -1 : 1;
-    return 0;
-}
-void ORC(set_resolve_ties)(int on) { g_resolve_ties = on && sizeof(real) == 4; }
-int ORC(tie_table_set)(const uint32_t *keys, const uint32_t *vals, int n) {
-    free(g_tie_tab);
-    g_tie_tab = NULL;
-    g_tie_tab_n = 0;
-    if (n <= 0) return 0;
-    g_tie_tab = (tie_entry *)malloc(sizeof(tie_entry) * (size_t)n);
-    if (!g_tie_tab) return 1;
-    for (int i = 0; i < n; ++i) {
-        memcpy(g_tie_tab[i].k, keys + 4 * (size_t)i, 16);
-        g_tie_tab[i].v = vals[i];
-    }
-    qsort(g_tie_tab, (size_t)n, sizeof(tie_entry), tie_key_cmp);
-    g_tie_tab_n = n;
-    return 0;
-}
-int ORC(tie_log_count)(void) { return g_tie_log_n; }
-/* Copies up to max logged keys (4 words each) into out and empties the log;
- * returns how many were logged. */
-int ORC(tie_log_take)(uint32_t *out, int max) {
-    const int n = g_tie_log_n;
-    if (out) memcpy(out, g_tie_log, sizeof(uint32_t) * 4 * (size_t)(n < max ? n : max));
-    g_tie_log_n = 0;
-    return n;
-}
-static int tie_lookup(uint32_t kind, float a, float b, float c, uint32_t *v) {
-    uint32_t k[4] = {kind, 0, 0, 0};
-    memcpy(&k[1], &a, 4);
-    memcpy(&k[2], &b, 4);
-    memcpy(&k[3], &c, 4);
-    const tie_entry *e = g_tie_tab_n ? (const tie_entry *)bsearch(k, g_tie_tab, (size_t)g_tie_tab_n, sizeof(tie_entry),
-                                                                  tie_key_cmp)
-                                     : NULL;
-    if (e) {
-        *v = e->v;
-        return 1;
-    }
-#pragma omp critical(orc_tie_log)
-    {
-        if (g_tie_log_n == g_tie_log_cap) {
-            const int cap = g_tie_log_cap ? 2 * g_tie_log_cap : 1024;
-            uint32_t *p = (uint32_t *)realloc(g_tie_log, sizeof(uint32_t) * 4 * (size_t)cap);
-            if (p) {
-                g_tie_log = p;
-                g_tie_log_cap = cap;
-            }
-        }
-        if (g_tie_log_n < g_tie_log_cap) memcpy(g_tie_log + 4 * (size_t)g_tie_log_n++, k, 16);
-    }
-    return 0;
+    return (int)(b & 1) == (g_flip_ties - 2) % 2;
 }
 
 /* __float2int_rn of a quotient, flagging (and, when flipping, reversing) a
@@ -581,19 +511,6 @@ static inline int round_q(real q, int *tie) {
     }
     return r;
 }
-/* __float2int_rn(num / den + add) as round_q, a tie resolved by the
- * reference's arithmetic when that is on and the operands are known. */
-static inline int round_div(real num, real den, real add, int *tie) {
-    const real q = num / den + add;
-    if (g_resolve_ties && near_half(q, TIE_REL, fabs((double)q) + 1.0)) {
-        uint32_t v;
-        if (tie_lookup(0, (float)num, (float)den, (float)add, &v)) {
-            *tie = 1;
-            return (int)v;
-        }
-    }
-    return round_q(q, tie);
-}
 /* a comparison result, reversed when flipping and its operands are a tie */
 static inline int decide(int result, double a, double t, int *tie) {
     if (near_thr(a, t, TIE_REL)) {
@@ -601,22 +518,6 @@ static inline int decide(int result, double a, double t, int *tie) {
         if (g_flip_ties && flip_this(a)) return !result;
     }
     return result;
-}
-/* sqrt(sq) < t (strict) or <= t, as decide, a tie resolved by the
- * reference's square root when that is on and the operand is known. */
-static inline int decide_sqrt(real sq, real t, int strict, int *tie) {
-    const real s = SQRT(sq);
-    const int result = strict ? s < t : s <= t;
-    if (g_resolve_ties && near_thr(s, t, TIE_REL)) {
-        uint32_t v;
-        if (tie_lookup(1, (float)sq, 0.f, 0.f, &v)) {
-            float g;
-            memcpy(&g, &v, 4);
-            *tie = 1;
-            return strict ? (real)g < t : (real)g <= t;
-        }
-    }
-    return decide(result, s, t, tie);
 }
 
 /* ------------------------------------------------------------------ */
@@ -837,9 +738,10 @@ static int icp_search(const icp_args *a, int x, int y, v3 *n, v3 *d, v3 *s, int 
     if (isnan_r(vcurr.x)) return 0; /* GPU: NaN -> (0,0) gather, then dist is NaN -> reject */
     v3 vcurr_g = add(mv(&a->Rcurr, vcurr), a->tcurr);
     v3 vcurr_cp = mv(&a->Rprev_inv, sub(vcurr_g, a->tprev));
+    real qx = vcurr_cp.x * a->fx / vcurr_cp.z + a->cx;
+    real qy = vcurr_cp.y * a->fy / vcurr_cp.z + a->cy;
     int tq = 0;
-    int ux = round_div(vcurr_cp.x * a->fx, vcurr_cp.z, a->cx, &tq);
-    int uy = round_div(vcurr_cp.y * a->fy, vcurr_cp.z, a->cy, &tq);
+    int ux = round_q(qx, &tq), uy = round_q(qy, &tq);
     if (tq) *tie |= 1;
     if (ux < 0 || uy < 0 || ux >= a->cols || uy >= a->rows || vcurr_cp.z < 0) return 0;
     const size_t q = (size_t)uy * a->cols + ux;
@@ -847,11 +749,12 @@ static int icp_search(const icp_args *a, int x, int y, v3 *n, v3 *d, v3 *s, int 
     v3 ncurr = mk(a->nmap_curr[p], a->nmap_curr[N + p], a->nmap_curr[2 * N + p]);
     v3 ncurr_g = mv(&a->Rcurr, ncurr);
     v3 nprev_g = mk(a->nmap_g_prev[q], a->nmap_g_prev[N + q], a->nmap_g_prev[2 * N + q]);
-    const v3 dv = sub(vprev_g, vcurr_g), cr = cross(ncurr_g, nprev_g);
+    real dist = norm3(sub(vprev_g, vcurr_g));
+    real sine = norm3(cross(ncurr_g, nprev_g));
     *n = nprev_g; *d = vprev_g; *s = vcurr_g;
     int tt = 0;
-    const int sine_ok = decide_sqrt(dot(cr, cr), a->angleThres, 1, &tt);    /* norm(cross) < angleThres */
-    const int dist_ok = decide_sqrt(dot(dv, dv), a->distThres, 0, &tt);     /* norm(diff) <= distThres */
+    const int sine_ok = decide(sine < a->angleThres, sine, a->angleThres, &tt);
+    const int dist_ok = decide(dist <= a->distThres, dist, a->distThres, &tt);
     if (tt) *tie |= 2;
     int ok = (sine_ok && dist_ok && !isnan_r(ncurr.x) && !isnan_r(nprev_g.x));
     if (ok) *idx = (int)q;
@@ -943,10 +846,10 @@ void ORC(rgb_residual)(real minScale, const int16_t *dIdx, const int16_t *dIdy, 
                     real d1 = nextDepth[y * cols + x];
                     if (!isnan_r(d1)) {
                         real td1 = d1 * (krkinv[6] * (real)x + krkinv[7] * (real)y + krkinv[8]) + kt[2];
-                        real nu = d1 * (krkinv[0] * (real)x + krkinv[1] * (real)y + krkinv[2]) + kt[0];
-                        real nv = d1 * (krkinv[3] * (real)x + krkinv[4] * (real)y + krkinv[5]) + kt[1];
+                        real qu = (d1 * (krkinv[0] * (real)x + krkinv[1] * (real)y + krkinv[2]) + kt[0]) / td1;
+                        real qv = (d1 * (krkinv[3] * (real)x + krkinv[4] * (real)y + krkinv[5]) + kt[1]) / td1;
                         int tq = 0;
-                        int u0 = round_div(nu, td1, 0, &tq), v0 = round_div(nv, td1, 0, &tq);
+                        int u0 = round_q(qu, &tq), v0 = round_q(qv, &tq);
                         if (tq) tf |= 1;
                         if (u0 >= 0 && v0 >= 0 && u0 < cols && v0 < rows) {
                             real d0 = lastDepth[v0 * cols + u0];
@@ -1050,7 +953,7 @@ void ORC(so3_step)(const uint8_t *lastImage, const uint8_t *nextImage, int cols,
             v3 p = mk((real)x, (real)y, 1);
             v3 wp = mv(&Hm, p);
             int tq = 0;
-            int wx = round_div(wp.x, wp.z, 0, &tq), wy = round_div(wp.y, wp.z, 0, &tq);
+            int wx = round_q(wp.x / wp.z, &tq), wy = round_q(wp.y / wp.z, &tq);
             int found = wx >= 1 && wx < cols - 1 && wy >= 1 && wy < rows - 1 && x >= 1 && x < cols - 1 && y >= 1 &&
                         y < rows - 1;
             real row[4] = {0, 0, 0, 0};

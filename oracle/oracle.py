@@ -274,32 +274,6 @@ def set_flip_ties(prec, mode):
     Kernels(prec).f("set_flip_ties")(int(mode))
 
 
-def set_resolve_ties(prec, on):
-    """Rounding ties of the per-pixel kernels (FP32 build) are decided by a
-    table of the reference's own division / square-root results where the
-    table has the operands (set_tie_table); unknown operands are logged
-    (take_tie_log) and decided in IEEE arithmetic."""
-    Kernels(prec).f("set_resolve_ties")(int(bool(on)))
-
-
-def take_tie_log(prec=32):
-    """[n, 4] uint32 keys (kind, a, b, c) of the ties met since the last
-    call whose operands were not in the table (may repeat)."""
-    k = Kernels(prec)
-    n = k.f("tie_log_count")()
-    out = np.zeros((max(n, 1), 4), np.uint32)
-    k.f("tie_log_take")(_p(out), n)
-    return out[:n]
-
-
-def set_tie_table(prec, keys, vals):
-    keys = np.ascontiguousarray(keys, np.uint32).reshape(-1, 4)
-    vals = np.ascontiguousarray(vals, np.uint32).reshape(-1)
-    assert len(keys) == len(vals)
-    if Kernels(prec).f("tie_table_set")(_p(keys), _p(vals), len(keys)) != 0:
-        raise MemoryError("tie table")
-
-
 def set_reverse_sums(prec, mode):
     """Summation-order perturbations of every pairwise sum of the given
     precision: 0 / False none, 1 / True records in reverse order, 2 another

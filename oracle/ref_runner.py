@@ -80,7 +80,7 @@ class RefKernels:
         self.fn = {}
         for key, name in list(K.items()) + [(n, n) for n in ("shim_icp_pixels", "shim_rgb_residual",
                                                             "shim_rgb_step", "shim_so3_pixels", "shim_set_rgba",
-                                                            "shim_warp_variants", "shim_arith")]:
+                                                            "shim_warp_variants")]:
             f = ctypes.c_void_p()
             self._ck(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
             self.fn[key] = f
@@ -305,18 +305,3 @@ class RefKernels:
                                                   ctypes.c_int(h), ctypes.c_void_p(par.data_ptr()),
                                                   ctypes.c_void_p(out.data_ptr())])
         return out
-
-    def arith(self, keys):
-        """The reference's division / square root on tie operands: keys
-        [n, 4] uint32 (kind, a, b, c bit patterns, see shim_arith) -> [n]
-        uint32 results."""
-        keys = np.ascontiguousarray(keys, np.uint32).reshape(-1, 4)
-        n = len(keys)
-        if n == 0:
-            return np.zeros(0, np.uint32)
-        k = self.torch.from_numpy(keys.view(np.int32)).cuda()
-        out = self._empty((n,), self.torch.int32)
-        g, b = self._grid1(n)
-        self._launch("shim_arith", g, b, [ctypes.c_void_p(k.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-                                          ctypes.c_int(n)])
-        return out.cpu().numpy().view(np.uint32)

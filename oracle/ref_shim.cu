@@ -213,23 +213,3 @@ extern "C" __global__ void shim_warp_variants(const float *nextDepth, int cols, 
         }
     }
 }
-
-// The reference's division and square root on given operands, for the
-// oracle's tie resolution: with --prec-div=false --prec-sqrt=false the
-// reference's `a / b` and sqrtf differ from IEEE by up to a few ulp, which
-// can move an integer rounding or a threshold test that the CPU oracle
-// evaluates in IEEE arithmetic.  keys[4 i .. 4 i + 3] = (kind, a, b, c) as
-// bit patterns:
-//   kind 0: __float2int_rn(a / b + c)  (the projections of ICPReduction::search,
-//           src/odom/reduce.cu:294-295, RGBResidual::getProducts :812-814,
-//           SO3Reduction::getProducts :983-984), out = the int;
-//   kind 1: sqrtf(a)  (norm(), src/cuda/operators.cuh:77-80), out = the bits.
-extern "C" __global__ void shim_arith(const unsigned *keys, unsigned *out, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned kind = keys[4 * i];
-    const float a = __uint_as_float(keys[4 * i + 1]), b = __uint_as_float(keys[4 * i + 2]),
-                c = __uint_as_float(keys[4 * i + 3]);
-    if (kind == 0) out[i] = (unsigned)__float2int_rn(a / b + c);
-    else out[i] = __float_as_uint(sqrtf(a));
-}

@@ -23,6 +23,10 @@
 #include "odo_internal.h"
 #include "se3_math.h"
 
+// The warm-start network's proposals enqueued on stream `st` instead of the
+// network's own (cnn_host.cpp); the batch runs them beside its preprocessing.
+extern "C" int cnn_propose_on(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_dev, cudaStream_t st);
+
 using namespace slamgb;
 
 namespace {
@@ -78,6 +82,11 @@ struct odo_batch {
     int last_n = 0, last_rgb = 0;  // pair count and photometric flag of the last tracking call
     bool follow_legacy = true;     // stream NULL: order after the legacy default stream's work
     cudaEvent_t order_ev = nullptr;
+    // warm start: the network's proposals run on side_stream beside the
+    // preprocessing; warm_ev marks their end and the tracking graph waits on
+    // it right before seeding the pairs (an external-event wait node)
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, warm_ev = nullptr;
     std::map<GKey, cudaGraphExec_t> graphs;
     std::string last_error;
 };
@@ -448,6 +457,7 @@ cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, con
         e = launch_derivatives_batch((const DerivArgs *)A(b->o_deriv), n, W, Hh, s);
     if (e == cudaSuccess && so3) e = launch_so3_batch((const So3Args *)A(b->o_so3), n, s);
     if (e == cudaSuccess) e = launch_track_begin_batch(b->st_dev, n, s);
+    if (e == cudaSuccess && warm) e = cudaStreamWaitEvent(s, b->warm_ev, cudaEventWaitExternal);
     if (e == cudaSuccess && warm) e = launch_warm_seed_batch(b->st_dev, b->init_dev, n, s);
     for (int l = kLevels - 1; l >= 0 && e == cudaSuccess; --l)
         for (int j = 0; j < max_iters[l] && e == cudaSuccess; ++j)
@@ -504,8 +514,12 @@ int odo_batch_create(int max_pairs, odo_batch_t **out) {
     std::memset(b->args_host, 0, o);
     if ((e = cudaMalloc(&b->st_dev, sizeof(TrackState) * np)) != cudaSuccess) return bail(e, "cudaMalloc(states)");
     if ((e = cudaMalloc(&b->init_dev, sizeof(float) * 6 * np)) != cudaSuccess) return bail(e, "cudaMalloc(init)");
-    if ((e = cudaEventCreateWithFlags(&b->order_ev, cudaEventDisableTiming)) != cudaSuccess)
+    if ((e = cudaEventCreateWithFlags(&b->order_ev, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->warm_ev, cudaEventDisableTiming)) != cudaSuccess)
         return bail(e, "cudaEventCreate");
+    if ((e = cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(e, "cudaStreamCreate(side)");
     if ((e = cudaMallocHost(&b->st_host, sizeof(TrackState) * np)) != cudaSuccess)
         return bail(e, "cudaMallocHost(states)");
     *out = b;
@@ -523,6 +537,12 @@ int odo_batch_destroy(odo_batch_t *b) {
     if (b->st_host) cudaFreeHost(b->st_host);
     if (b->init_dev) cudaFree(b->init_dev);
     if (b->order_ev) cudaEventDestroy(b->order_ev);
+    if (b->side_stream) {
+        cudaStreamSynchronize(b->side_stream);
+        cudaStreamDestroy(b->side_stream);
+    }
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->warm_ev) cudaEventDestroy(b->warm_ev);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
     return ODO_OK;
@@ -709,11 +729,18 @@ int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, 
                          const odo_warm_params *wp, odo_pair_result *results, int *fallback) {
     if (!b || !net || !pairs || !wp || !results || npairs < 1 || npairs > b->max_pairs) return ODO_ERR_ARG;
     if (wp->levels < 1 || wp->levels > 3) return ODO_ERR_ARG;
-    // 1. proposals straight into the warm-start buffer (network stream), then
-    //    the batch stream waits for them
-    int rc = odo_cnn_propose(net, pairs, npairs, b->init_dev);
+    // 1. proposals straight into the warm-start buffer, on the side stream
+    //    (after the work already on the batch stream); the tracking graph's
+    //    preprocessing runs beside them and its seeding waits for warm_ev
+    if (b->follow_legacy) {
+        BCK(cudaEventRecord(b->order_ev, 0));
+        BCK(cudaStreamWaitEvent(b->stream, b->order_ev, 0));
+    }
+    BCK(cudaEventRecord(b->fork_ev, b->stream));
+    BCK(cudaStreamWaitEvent(b->side_stream, b->fork_ev, 0));
+    int rc = cnn_propose_on(net, pairs, npairs, b->init_dev, b->side_stream);
     if (rc != ODO_OK) return rc;
-    BCK(cudaStreamWaitEvent(b->stream, (cudaEvent_t)odo_cnn_event(net), 0));
+    BCK(cudaEventRecord(b->warm_ev, b->side_stream));
     // 2. tracking from the proposals with the short schedule
     std::vector<odo_pair> warm(pairs, pairs + npairs);
     for (auto &q : warm) {

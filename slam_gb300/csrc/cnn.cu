@@ -59,6 +59,13 @@ struct LdDense {
         for (int j = 0; j < 8; ++j) v[j] = (k + j < K) ? q[k + j] : 0;
         return pack8(v);
     }
+    // the same slot for the asynchronously fed GEMM (a partial last K group
+    // copies its valid bytes and zero-fills the rest)
+    __device__ const void *src(Row q, int k, int &bytes) const {
+        const int n = (q && k < K) ? min(8, K - k) : 0;
+        bytes = 2 * n;
+        return n ? static_cast<const void *>(q + k) : static_cast<const void *>(p);
+    }
 };
 // Row-major FP32 [rows][ld] rounded to BF16.
 struct LdDenseF32 {
@@ -145,6 +152,12 @@ struct LdIm2col {
     using Col = int4;
     __device__ Row row(int m) const { return g.pos(m); }
     __device__ Col col(int k8) const { return g.tap(k8 * 8); }
+    __device__ const void *src(const int4 &p, const int4 &t, int &bytes) const {
+        static_assert(!F16, "the asynchronously fed GEMM copies the 16-bit values unconverted");
+        const long long o = g.src(p, t);
+        bytes = o < 0 ? 0 : 16;
+        return o < 0 ? static_cast<const void *>(x) : static_cast<const void *>(x + o);
+    }
     __device__ uint4 load(const int4 &p, const int4 &t) const {
         const long long o = g.src(p, t);
         if (o < 0) return zero4();
@@ -453,6 +466,15 @@ cudaError_t gemm(const LA &a, const LB &b, const EP &e, int M, int N, int K, int
     return launch_umma_gemm<128, LA, LB, EP, F16>(a, b, e, M, N, K, splits, 0, err, s);
 }
 
+// Forward products: operands copied into shared memory by cp.async, four
+// K chunks in flight (k_umma_gemm_async).
+template <bool F16 = false, class LA, class LB, class EP>
+cudaError_t gemm_async(const LA &a, const LB &b, const EP &e, int M, int N, int K, int *err, cudaStream_t s) {
+    if (N <= 32) return launch_umma_gemm_async<32, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);
+    if (N <= 64) return launch_umma_gemm_async<64, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);
+    return launch_umma_gemm_async<128, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);
+}
+
 }  // namespace
 
 #define CNN_CK(x)                              \
@@ -468,14 +490,16 @@ cudaError_t cnn_forward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
         const int M = B * g.Ho * g.Wo, N = kCout[l], K = w_cols(l);
         const EpBiasAct ep{n.act[l + 1], n.master + P.b[l], N, N, 1};
         // the first layer in FP16 (the FP16 depth keeps 11 significant bits)
-        if (l == 0) CNN_CK(gemm<true>(LdIm2col<false>{input, g}, LdDense{n.wh, N, K, K}, ep, M, N, K, 1, n.err, s));
-        else CNN_CK(gemm(LdIm2col<false>{n.act[l], g}, LdDense{n.wbf + P.w[l], N, K, K}, ep, M, N, K, 1, n.err, s));
+        if (l == 0)
+            CNN_CK(gemm_async<true>(LdIm2col<false>{input, g}, LdDense{n.wh, N, K, K}, ep, M, N, K, n.err, s));
+        else
+            CNN_CK(gemm_async(LdIm2col<false>{n.act[l], g}, LdDense{n.wbf + P.w[l], N, K, K}, ep, M, N, K, n.err, s));
     }
     const int l1 = kConv, l2 = kConv + 1;
-    CNN_CK(gemm(LdDense{n.act[kConv], B, kFlat, kFlat}, LdDense{n.wbf + P.w[l1], kHidden, kFlat, kFlat},
-                EpBiasAct{n.hid, n.master + P.b[l1], kHidden, kHidden, 1}, B, kHidden, kFlat, 1, n.err, s));
-    CNN_CK(gemm(LdDense{n.hid, B, kHidden, kHidden}, LdDense{n.wbf + P.w[l2], kOut, kHidden, kHidden},
-                EpBiasF32{n.out, n.master + P.b[l2], kOut, kOut}, B, kOut, kHidden, 1, n.err, s));
+    CNN_CK(gemm_async(LdDense{n.act[kConv], B, kFlat, kFlat}, LdDense{n.wbf + P.w[l1], kHidden, kFlat, kFlat},
+                      EpBiasAct{n.hid, n.master + P.b[l1], kHidden, kHidden, 1}, B, kHidden, kFlat, n.err, s));
+    CNN_CK(gemm_async(LdDense{n.hid, B, kHidden, kHidden}, LdDense{n.wbf + P.w[l2], kOut, kHidden, kHidden},
+                      EpBiasF32{n.out, n.master + P.b[l2], kOut, kOut}, B, kOut, kHidden, n.err, s));
     return cudaSuccess;
 }
 
@@ -563,6 +587,12 @@ cudaError_t cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M
                            int *err, cudaStream_t s) {
     const LdDense la{A, M, K, (K + 7) & ~7}, lb{B, N, K, (K + 7) & ~7};
     const EpStore ep{C, N, N};
+    if (layout == 8) {  // the asynchronously fed kernel (BF16)
+        if (bn == 32) return launch_umma_gemm_async<32>(la, lb, ep, M, N, K, err, s);
+        if (bn == 64) return launch_umma_gemm_async<64>(la, lb, ep, M, N, K, err, s);
+        if (bn == 128) return launch_umma_gemm_async<128>(la, lb, ep, M, N, K, err, s);
+        return launch_umma_gemm_async<256>(la, lb, ep, M, N, K, err, s);
+    }
     if ((layout & 3) == 2) {  // FP16 operands
         const int lay = layout & 4;
         if (bn == 32) return launch_umma_gemm<32, LdDense, LdDense, EpStore, true>(la, lb, ep, M, N, K, 1, lay, err, s);

@@ -59,6 +59,7 @@ int check_timeout(odo_cnn_t *n) {
     if (flag) {
         n->err = "tensor-core pipeline wait timed out";
         CCK(cudaMemsetAsync(n->net.err, 0, sizeof(int), n->stream));
+        CCK(cudaStreamSynchronize(n->stream));
         return ODO_ERR_TIMEOUT;
     }
     return ODO_OK;
@@ -248,7 +249,14 @@ int odo_cnn_forward(odo_cnn_t *n, const uint16_t *input, int batch, float *out) 
     return check_timeout(n);
 }
 
+static int pack_input_on(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t *input_dev, cudaStream_t s);
+
 int odo_cnn_pack_input(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t *input_dev) {
+    if (!n) return ODO_ERR_ARG;
+    return pack_input_on(n, pairs, npairs, input_dev, n->stream);
+}
+
+static int pack_input_on(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t *input_dev, cudaStream_t s) {
     if (!n || !pairs || !input_dev || npairs < 1 || npairs > n->net.max_batch) return ODO_ERR_ARG;
     CCK(cudaEventSynchronize(n->pack_done));
     for (int i = 0; i < npairs; ++i) {
@@ -262,27 +270,31 @@ int odo_cnn_pack_input(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16_t
                                    q.depth,       q.depth_pitch, q.rgba,       q.rgba_pitch,
                                    sc};
     }
-    CCK(cudaMemcpyAsync(n->pack_dev, n->pack_host, sizeof(PackArgs) * npairs, cudaMemcpyHostToDevice, n->stream));
-    CCK(cudaEventRecord(n->pack_done, n->stream));
-    CCK(cnn_pack(n->pack_dev, npairs, input_dev, n->stream));
+    CCK(cudaMemcpyAsync(n->pack_dev, n->pack_host, sizeof(PackArgs) * npairs, cudaMemcpyHostToDevice, s));
+    CCK(cudaEventRecord(n->pack_done, s));
+    CCK(cnn_pack(n->pack_dev, npairs, input_dev, s));
     return ODO_OK;
 }
 
-int odo_cnn_propose(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_dev) {
+int cnn_propose_on(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_dev, cudaStream_t st) {
     if (!n || !pairs || !out_dev || npairs < 1) return ODO_ERR_ARG;
     Net &N = n->net;
     if (!n->in_buf) CCK(cudaMalloc(&n->in_buf, (size_t)N.max_batch * kInH * kInW * kInC * 2));
     for (int s = 0; s < npairs; s += N.max_batch) {
         const int m = npairs - s < N.max_batch ? npairs - s : N.max_batch;
-        int rc = odo_cnn_pack_input(n, pairs + s, m, n->in_buf);
+        int rc = pack_input_on(n, pairs + s, m, n->in_buf, st);
         if (rc != ODO_OK) return rc;
-        CCK(cnn_forward(N, n->in_buf, m, n->stream));
-        CCK(cudaMemcpyAsync(out_dev + (size_t)6 * s, N.out, (size_t)m * kOut * 4, cudaMemcpyDeviceToDevice,
-                            n->stream));
+        CCK(cnn_forward(N, n->in_buf, m, st));
+        CCK(cudaMemcpyAsync(out_dev + (size_t)6 * s, N.out, (size_t)m * kOut * 4, cudaMemcpyDeviceToDevice, st));
     }
-    CCK(cudaMemcpyAsync(n->flag_host, N.err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
-    CCK(cudaEventRecord(n->done, n->stream));
+    CCK(cudaMemcpyAsync(n->flag_host, N.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CCK(cudaEventRecord(n->done, st));
     return ODO_OK;
+}
+
+int odo_cnn_propose(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_dev) {
+    if (!n) return ODO_ERR_ARG;
+    return cnn_propose_on(n, pairs, npairs, out_dev, n->stream);
 }
 
 void *odo_cnn_event(odo_cnn_t *n) { return n ? (void *)n->done : nullptr; }
@@ -328,7 +340,8 @@ int odo_cnn_train_step(odo_cnn_t *n, const uint16_t *input, const float *labels,
 
 int odo_cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M, int N, int K, int bn, int layout,
                        void *stream) {
-    if (!A || !B || !C || M < 1 || N < 1 || K < 1 || (layout & 3) > 2 || layout < 0 || layout > 6) return ODO_ERR_ARG;
+    if (!A || !B || !C || M < 1 || N < 1 || K < 1 || (layout & 3) > 2 || layout < 0 || (layout > 6 && layout != 8))
+        return ODO_ERR_ARG;
     if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return ODO_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     int *err = nullptr;

@@ -145,6 +145,167 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm(LA la, LB lb, EP ep,
     if (warp == 0) umma::tmem_dealloc(tmem, BN < 32 ? 32 : BN);
 }
 
+// ---------------------------------------------------------------------------
+// Asynchronously fed variant.  The operand slots go from global memory
+// straight into the stage buffers by cp.async (no register staging): the
+// loaders name the source of each 16-byte slot,
+//   __device__ const void *src(const Row &, const Col &, int &bytes) const;
+// (bytes < 16 zero-fills the rest of the slot; bytes = 0 reads nothing and
+// the returned address only has to be a valid one), and S stages of K chunks
+// are in flight while the MMAs of the oldest run.  Stage s of chunk c is
+// refilled with chunk c + S once the MMAs of chunk c have completed (their
+// commit on mbar[s]).  Every wait is bounded like the register-staged
+// kernel's; whatever stops the loop, the kernel waits (bounded) for its own
+// copies and MMAs before it releases TMEM.
+template <int BN, int S>
+constexpr int gemm_async_smem_bytes() {
+    return S * (128 * kGemmKChunk * 2 + BN * kGemmKChunk * 2) + 1024;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(umma::smem_u32(smem)), "l"(gmem), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_group() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_groups() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int BN, bool F16, int S, class LA, class LB, class EP>
+__global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, EP ep, int M, int N, int kchunks,
+                                                                  int chunks_per_split, int *err) {
+    static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "BN");
+    static_assert(S >= 2 && S <= 6, "stages");
+    constexpr int A_BYTES = 128 * kGemmKChunk * 2, B_BYTES = BN * kGemmKChunk * 2, STAGE = A_BYTES + B_BYTES;
+    constexpr uint32_t IDESC = F16 ? umma::idesc_f16_f32(128, BN) : umma::idesc_bf16_f32(128, BN);
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t mbar[S];
+    __shared__ uint32_t tmem_base;
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+    const int c_begin = blockIdx.z * chunks_per_split;
+    const int c_end = min(kchunks, c_begin + chunks_per_split);
+    const int nch = c_end - c_begin;
+    if (nch <= 0) return;
+    if (warp == 0) {
+        umma::tmem_alloc(&tmem_base, BN < 32 ? 32 : BN);
+        umma::tmem_relinquish();
+    }
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) umma::mbar_init(&mbar[s], 1);
+        umma::mbar_fence_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    // slots as in k_umma_gemm: thread t fills the 16-byte slots t + 128 j
+    constexpr int AR = 8, BR = BN / 16;
+    const int kg = (tid >> 3) & 7;
+    typename LA::Row ra[AR];
+    typename LB::Row rb[BR];
+#pragma unroll
+    for (int j = 0; j < AR; ++j) ra[j] = la.row(m0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
+#pragma unroll
+    for (int j = 0; j < BR; ++j) rb[j] = lb.row(n0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
+    auto issue = [&](int c) {
+        uint8_t *sa = smem + (c % S) * STAGE;
+        uint8_t *sb = sa + A_BYTES;
+        const int k8 = (c_begin + c) * (kGemmKChunk / 8) + kg;
+        const typename LA::Col ca = la.col(k8);
+#pragma unroll
+        for (int j = 0; j < AR; ++j) {
+            int bytes;
+            const void *g = la.src(ra[j], ca, bytes);
+            cp_async16(sa + (tid + 128 * j) * 16, g, bytes);
+        }
+        const typename LB::Col cb = lb.col(k8);
+#pragma unroll
+        for (int j = 0; j < BR; ++j) {
+            int bytes;
+            const void *g = lb.src(rb[j], cb, bytes);
+            cp_async16(sb + (tid + 128 * j) * 16, g, bytes);
+        }
+    };
+#pragma unroll
+    for (int p = 0; p < S - 1; ++p) {
+        if (p < nch) issue(p);
+        cp_async_group();
+    }
+    bool ok = true;
+    int c = 0;
+    for (; c < nch; ++c) {
+        const int s = c % S;
+        // refill the stage the MMAs of chunk c - 1 read, with chunk c + S - 1
+        const int pf = c + S - 1;
+        if (pf < nch) {
+            if (c >= 1) {
+                ok = umma::mbar_wait(&mbar[(c - 1) % S], ((c - 1) / S) & 1, kGemmWaitPolls);
+                if (!__syncthreads_and(ok)) break;
+            }
+            issue(pf);
+        }
+        cp_async_group();
+        cp_async_wait_groups<S - 1>();  // this thread's copies of chunk c have landed
+        umma::fence_smem_to_async();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            const uint32_t a0 = umma::smem_u32(smem + s * STAGE), b0 = a0 + A_BYTES;
+#pragma unroll
+            for (int k = 0; k < kGemmKChunk / 16; ++k)
+                umma::mma_bf16(tmem, umma::smem_desc(a0 + k * 256, 128u, 1024u),
+                               umma::smem_desc(b0 + k * 256, 128u, 1024u), IDESC, (c > 0 || k > 0) ? 1u : 0u);
+            umma::mma_commit(&mbar[s]);
+        }
+    }
+    cp_async_wait_groups<0>();
+    bool drained = true;
+    if (c > 0) {
+        const int last = c - 1;
+        drained = umma::mbar_wait(&mbar[last % S], (last / S) & 1, kGemmWaitPolls);
+    }
+    ok = __syncthreads_and(ok && drained) && c == nch;
+    umma::fence_after_sync();
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int j = 0; j < BN; j += 8) {
+            float v[8];
+            umma::tmem_ld8(trow + j, v);
+            if (row < M && n0 + j < N) ep(row, n0 + j, v);
+        }
+    } else if (tid == 0 && err) {
+        atomicExch(err, 1);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, BN < 32 ? 32 : BN);
+}
+
+template <int BN, class LA, class LB, class EP, bool F16 = false, int S = 4>
+cudaError_t launch_umma_gemm_async(const LA &la, const LB &lb, const EP &ep, int M, int N, int K, int *err,
+                                   cudaStream_t s) {
+    if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+    const int kchunks = (K + kGemmKChunk - 1) / kGemmKChunk;
+    constexpr int smem = gemm_async_smem_bytes<BN, S>();
+    static bool attr_set = false;  // per instantiation
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_async<BN, F16, S, LA, LB, EP>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dim3 grid((M + 127) / 128, (N + BN - 1) / BN, 1);
+    k_umma_gemm_async<BN, F16, S, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, kchunks,
+                                                                              err);
+    return cudaGetLastError();
+}
+
 // Host-side launch helper (in a .cu translation unit).
 template <int BN, class LA, class LB, class EP, bool F16 = false>
 cudaError_t launch_umma_gemm(const LA &la, const LB &lb, const EP &ep, int M, int N, int K, int splits, int layout,

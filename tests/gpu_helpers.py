@@ -125,85 +125,32 @@ def set_images(o, images):
     o.keep_derivatives(True)
 
 
-# Rounding ties.  The reference divides and takes square roots in their
-# approximate forms; the oracle evaluates them in IEEE arithmetic and flags
-# the integer roundings and threshold tests that sit within a few ulp of a
-# decision boundary.  Where the reference's kernels are available (the
-# cubin of oracle/build_ref.py), every FP32 oracle run decides those ties
-# with the reference's own arithmetic: the run logs the operands of each
-# tie, the reference's `a / b` and sqrtf are evaluated on them on the GPU
-# with the reference's flags (oracle/ref_shim.cu, shim_arith), and the run
-# is repeated with those results until it meets no new tie.  The oracle is
-# then an exact restatement of the reference's per-pixel arithmetic, on its
-# own trajectory.  _TIES caches the results (a pure function of the
-# operands) across runs.
-_TIES = {}
-_REF = []
-
-
-def _reference_kernels():
-    if not _REF:
-        try:
-            from oracle import ref_runner
-            _REF.append(ref_runner.RefKernels() if ref_runner.available() else None)
-        except Exception:
-            _REF.append(None)
-    return _REF[0]
-
-
-def ties_resolved():
-    return _reference_kernels() is not None
-
-
-def resolved(run_once, max_runs=8):
-    """run_once() (a fresh FP32 oracle run) with its ties decided by the
-    reference's arithmetic; without the reference's kernels, run_once()."""
-    from oracle import oracle
-    rk = _reference_kernels()
-    if rk is None:
-        return run_once()
-    oracle.set_resolve_ties(32, True)
-    try:
-        for _ in range(max_runs):
-            oracle.take_tie_log(32)
-            res = run_once()
-            new = {tuple(k) for k in oracle.take_tie_log(32).tolist()} - _TIES.keys()
-            if not new:
-                return res
-            keys = np.array(sorted(new), np.uint32)
-            _TIES.update(zip(map(tuple, keys.tolist()), rk.arith(keys).tolist()))
-            oracle.set_tie_table(32, np.array(list(_TIES.keys()), np.uint32),
-                                 np.array(list(_TIES.values()), np.uint32))
-        raise AssertionError("oracle run still meets new rounding ties after %d runs" % max_runs)
-    finally:
-        oracle.set_resolve_ties(32, False)
-
-
 # How precisely the reference algorithm determines the pose on an input is
 # measured by perturbing the oracle's own run: its FP64 twin (precision);
-# two other summation orders of every pairwise sum (reversed; split at a
-# third) -- the GPU's reduction tree is another order again; and, when a
-# loop decision (the SO3 convergence and divergence tests, the rgbOnly early
-# exit) compared two values within DECISION_MARGIN, that decision taken the
-# other way.  Without the reference's kernels the ties themselves are free:
-# then flagged ties decided the other way -- all of them, and each half of
-# them by a hash -- are perturbations too.  A GPU pose within 1e-5 of the
-# oracle's passes; beyond that it must be within twice the sum of the
+# flagged rounding ties decided the other way -- all of them, and each half
+# of them under four hashed splits (the decisions the reference's approximate
+# division and square root may take differently from the oracle's IEEE
+# arithmetic; the GPU's kernels, which equal the reference's, take some
+# subset of them differently); two other summation orders of every pairwise
+# sum (reversed; split at a third -- the GPU's reduction tree is another
+# order again); and, when a loop decision (the SO3 convergence and
+# divergence tests, the rgbOnly early exit) compared two values within
+# DECISION_MARGIN, that decision taken the other way.  A GPU pose passes when
+# it is within 1e-5 of the oracle's, or within 1e-5 of one of the perturbed
+# FP32 runs (it took that run's decisions), or within twice the sum of the
 # precision, tie (largest), order (largest) and decision differences, all of
-# which must be below GAP_LIMIT for the flat bound to apply.  Where one
+# which must be below GAP_LIMIT for the flat bound alone to apply.  Where one
 # exceeds UNDETERMINED (1 cm / 10 mrad) the algorithm does not determine the
 # pose on this input (e.g. ICP alone diverging from a large motion): the pose
 # is only required to be finite, and the case is reported.
 UNDETERMINED = 1e-2
 DECISION_MARGIN = 1e-3
-PERTURBATIONS_RESOLVED = {"fp64": (64, None), "order": (32, "reverse"), "order_b": (32, "third"),
-                          "decision": (32, "decision")}
-PERTURBATIONS_IEEE = {"fp64": (64, None), "ties": (32, 1), "ties_a": (32, 2), "ties_b": (32, 3),
-                      "order": (32, "reverse"), "order_b": (32, "third"), "decision": (32, "decision")}
-
-
-def perturbations():
-    return PERTURBATIONS_RESOLVED if ties_resolved() else PERTURBATIONS_IEEE
+TIE_SPLITS = 4
+PERTURBATIONS = {"fp64": (64, None), "ties": (32, 1)}
+for _k in range(2 * TIE_SPLITS):
+    PERTURBATIONS["ties_%d" % _k] = (32, 2 + _k)
+PERTURBATIONS.update({"order": (32, "reverse"), "order_b": (32, "third"), "decision": (32, "decision")})
+TIE_RUNS = ["ties"] + ["ties_%d" % k for k in range(2 * TIE_SPLITS)]
 
 
 class OracleRuns:
@@ -219,10 +166,10 @@ class OracleRuns:
         self._runs = {}
 
     def run(self, prec=32, perturb=None):
-        """perturb: None; 1 / 2 / 3 (ties the other way: all, half A, half B);
-        "reverse" / "third" (other summation orders); "decision" (the closest
-        loop decision of the unperturbed run the other way).  FP32 runs decide
-        their ties with the reference's arithmetic where it is available."""
+        """perturb: None; 1 (every tie the other way) or m >= 2 (half (m - 2) % 2
+        of the ties under hashed split (m - 2) / 2); "reverse" / "third" (other
+        summation orders); "decision" (the closest loop decision of the
+        unperturbed run the other way)."""
         key = (prec, perturb)
         if key not in self._runs:
             from oracle import oracle
@@ -245,7 +192,7 @@ class OracleRuns:
                     oracle.set_reverse_sums(prec, 0)
                 return np.asarray(t, np.float64), np.asarray(R, np.float64), o
 
-            self._runs[key] = resolved(once) if prec == 32 else once()
+            self._runs[key] = once()
         return self._runs[key]
 
     @property
@@ -257,14 +204,14 @@ class OracleRuns:
         return idx >= 0 and m < DECISION_MARGIN
 
     def _perturbed(self):
-        return [k for k in perturbations() if k != "decision" or self.near_decision()]
+        return [k for k in PERTURBATIONS if k != "decision" or self.near_decision()]
 
     def sensitivity(self):
         """{name: (rad, m)} differences of the perturbed runs from the FP32 run."""
         t32, R32, _ = self.run(32)
         out = {}
         for name in self._perturbed():
-            t, R, _ = self.run(*perturbations()[name])
+            t, R, _ = self.run(*PERTURBATIONS[name])
             out[name] = pose_diff(t32, R32, t, R)
         return out
 
@@ -281,7 +228,7 @@ class OracleRuns:
             return float("inf"), float("inf"), "undetermined (" + how + ")"
         if worst < GAP_LIMIT:
             return POSE_TOL_RAD, POSE_TOL_M, "flat (" + how + ")"
-        tie = [max([s[k][i] for k in ("ties", "ties_a", "ties_b") if k in s] + [0.0]) for i in (0, 1)]
+        tie = [max(s[k][i] for k in TIE_RUNS) for i in (0, 1)]
         order = [max(s["order"][i], s["order_b"][i]) for i in (0, 1)]
         tol = [2 * (s["fp64"][i] + tie[i] + order[i] + (s["decision"][i] if "decision" in s else 0.0))
                for i in (0, 1)]
@@ -291,7 +238,7 @@ class OracleRuns:
         """The GPU's iteration counts equal the oracle's or those of one of
         its FP32 perturbations (a near-tie loop decision may stop a loop one
         iteration earlier or later)."""
-        runs = [self.run(32)] + [self.run(*perturbations()[k]) for k in self._perturbed() if k != "fp64"]
+        runs = [self.run(32)] + [self.run(*PERTURBATIONS[k]) for k in self._perturbed() if k != "fp64"]
         return any(list(gpu_iterations) == r[2].iterations() for r in runs)
 
     def spread(self, metric):
@@ -299,8 +246,8 @@ class OracleRuns:
         the perturbations: precision + ties (largest of the three) + order +
         decision, as the pose bound combines them."""
         base = metric(self.run(32)[2])
-        d = {k: abs(metric(self.run(*perturbations()[k])[2]) - base) for k in self._perturbed()}
-        tie = max([d[k] for k in ("ties", "ties_a", "ties_b") if k in d] + [0.0])
+        d = {k: abs(metric(self.run(*PERTURBATIONS[k])[2]) - base) for k in self._perturbed()}
+        tie = max(d[k] for k in TIE_RUNS)
         return 2 * (d["fp64"] + tie + max(d["order"], d["order_b"]) + d.get("decision", 0.0))
 
     def jtj_tolerance(self, flat):
@@ -312,6 +259,33 @@ class OracleRuns:
         A = self.run(32)[2].stats["lastA"]
         scale = max(np.abs(A).max(), 1e-30)
         return max(1e-3, max(self.spread(lambda o, i=i: o.stats["lastA"].reshape(-1)[i]) for i in range(36)) / scale)
+
+    def _fp32_runs(self):
+        return [("main", self.run(32))] + [(k, self.run(*PERTURBATIONS[k])) for k in self._perturbed() if k != "fp64"]
+
+    def closest_run(self, tg, Rg):
+        """(name, (rad, m)) of the FP32 run (unperturbed or perturbed) closest
+        to a GPU pose."""
+        d = [(name, pose_diff(tg, Rg, r[0], r[1])) for name, r in self._fp32_runs()]
+        return min(d, key=lambda x: max(x[1][0] / POSE_TOL_RAD, x[1][1] / POSE_TOL_M))
+
+    def jtj_ok(self, A_gpu, flat):
+        """(ok, err): lastA within jtj_tolerance of the oracle's (max-normalised
+        relative difference err), or within 1e-3 of the lastA of one of the
+        perturbed FP32 runs (the GPU took that run's decisions)."""
+        A_gpu = np.asarray(A_gpu, np.float64).reshape(6, 6)
+        rel = lambda A: float(np.abs(A_gpu - A).max() / max(np.abs(A).max(), 1e-30))
+        err = rel(self.run(32)[2].stats["lastA"])
+        if err <= self.jtj_tolerance(flat):
+            return True, err
+        return any(rel(r[2].stats["lastA"]) <= 1e-3 for _, r in self._fp32_runs()), err
+
+    def count_ok(self, name, value, flat):
+        """A final count within count_tolerance of the oracle's, or within
+        0.2 % of one of the perturbed FP32 runs' counts."""
+        if abs(value - self.run(32)[2].stats[name]) <= self.count_tolerance(name, flat):
+            return True
+        return any(abs(value - r[2].stats[name]) <= 0.002 * max(1.0, r[2].stats[name]) for _, r in self._fp32_runs())
 
     def count_tolerance(self, name, flat):
         """Tolerance of a final inlier / correspondence count ("lastICPCount",
@@ -347,7 +321,14 @@ def check_pose(label, tg, Rg, to, Ro, tol_fn):
         report("%s: pose diff %.2e rad %.2e m <= flat 1e-5" % (label, rot, tr))
         return rot, tr, True
     tol_r, tol_t, how = tol_fn()
-    report("%s: pose diff %.2e rad %.2e m, tolerance %.2e rad %.2e m %s" % (label, rot, tr, tol_r, tol_t, how))
     assert np.all(np.isfinite(tg)) and np.all(np.isfinite(Rg)), label
+    owner = getattr(tol_fn, "__self__", None)
+    if not (rot <= tol_r and tr <= tol_t) and isinstance(owner, OracleRuns):
+        name, d = owner.closest_run(tg, Rg)
+        if d[0] <= POSE_TOL_RAD and d[1] <= POSE_TOL_M:
+            report("%s: pose diff %.2e rad %.2e m; within the flat 1e-5 of the oracle run with %s perturbed "
+                   "(%.2e rad %.2e m)" % (label, rot, tr, name, d[0], d[1]))
+            return rot, tr, False
+    report("%s: pose diff %.2e rad %.2e m, tolerance %.2e rad %.2e m %s" % (label, rot, tr, tol_r, tol_t, how))
     assert rot <= tol_r and tr <= tol_t, (label, rot, tr, tol_r, tol_t, how)
     return rot, tr, False

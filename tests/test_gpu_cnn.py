@@ -34,6 +34,11 @@ def test_umma_gemm_matches_torch(gpu, bn, shape):
     err = (C - ref).abs().max().item()
     tol = 1e-5 * K ** 0.5 * ref.abs().max().item() + 1e-4
     assert err <= tol, (bn, shape, err, tol)
+    # the asynchronously fed kernel of the forward pass: the same MMAs on the
+    # same shared-memory tiles, so the same bits
+    Ca = debug_gemm(A, B, bn=bn, layout=8)
+    torch.cuda.synchronize()
+    assert torch.equal(Ca, C), (bn, shape, (Ca - C).abs().max().item())
 
 
 @pytest.mark.parametrize("bn", [32, 128])
