@@ -53,7 +53,7 @@ BYTES_PER_PX_ITER = 62  # ICP 48 B (4 maps x 12 B) + photometric 14 B per pixel-
 RECORD_BYTES_PER_PX = 16
 # one-kernel ncu captures of this build whose `dram_bytes_per_px:` lines give
 # the measured traffic per pixel (traffic grows with the pixels processed)
-TRAFFIC_PROFILE_BATCH = "k_icp_rgbres_b_L0_48pairs_640x480.md"
+TRAFFIC_PROFILE_BATCH = "k_icp_rgbres_b_L0_24pairs_640x480.md"
 TRAFFIC_PROFILE_SINGLE = "k_icp_rgbres_L0_single_640x480.md"
 PREPROC_BYTES_PER_PX = 140  # per-frame map/pyramid building, per level-0 pixel (x 4/3 over the pyramid)
 
@@ -1258,7 +1258,8 @@ def run_warm_study(args):
                                    "max_disagree_deg": args.max_disagree}},
            "plain_batched_fps": n / (t_plain * 1e-3), "warm_batched_fps": n / (t_warm * 1e-3),
            "plain_single_pair_fps": single_fps,
-           "speedup_vs_plain_batched": t_plain / t_warm, "speedup_vs_plain_single": n / (t_warm * 1e-3) / single_fps,
+           "speedup_vs_plain_batched": t_plain / t_warm,
+           "speedup_vs_plain_single": n / (t_warm * 1e-3) / single_fps if single_fps else None,
            "pose_error_vs_gt": {"plain": {"rot_rad": pct(err_p[:, 0]), "trans_m": pct(err_p[:, 1]), "fail": fail(err_p)},
                                 "warm": {"rot_rad": pct(err_w[:, 0]), "trans_m": pct(err_w[:, 1]), "fail": fail(err_w)}},
            "warm_vs_plain": {"within_1e-5": float(np.mean((d[:, 0] <= 1e-5) & (d[:, 1] <= 1e-5))),

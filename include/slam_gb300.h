@@ -505,7 +505,7 @@ int odo_synth_render(const void *scenes_host, int nscenes, const int *view_scene
  * runs out on a barrier that nothing arrives at; returns ODO_ERR_TIMEOUT
  * after draining the issued MMAs; needs K > 128); layout = 8: the kernel
  * the network's forward pass uses (operands copied into shared memory by
- * cp.async, four K chunks in flight), BF16, library layout. */
+ * cp.async, a few K chunks in flight), BF16, library layout. */
 int odo_cnn_debug_gemm(const uint16_t *A_dev, const uint16_t *B_dev, float *C_dev, int M, int N, int K, int bn,
                        int layout, void *stream);
 

@@ -466,8 +466,8 @@ cudaError_t gemm(const LA &a, const LB &b, const EP &e, int M, int N, int K, int
     return launch_umma_gemm<128, LA, LB, EP, F16>(a, b, e, M, N, K, splits, 0, err, s);
 }
 
-// Forward products: operands copied into shared memory by cp.async, four
-// K chunks in flight (k_umma_gemm_async).
+// Forward products: operands copied into shared memory by cp.async, a few
+// K chunks in flight per CTA (k_umma_gemm_async).
 template <bool F16 = false, class LA, class LB, class EP>
 cudaError_t gemm_async(const LA &a, const LB &b, const EP &e, int M, int N, int K, int *err, cudaStream_t s) {
     if (N <= 32) return launch_umma_gemm_async<32, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);

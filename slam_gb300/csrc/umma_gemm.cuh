@@ -287,7 +287,14 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
     if (warp == 0) umma::tmem_dealloc(tmem, BN < 32 ? 32 : BN);
 }
 
-template <int BN, class LA, class LB, class EP, bool F16 = false, int S = 4>
+// Stages of K chunks per CTA (compile-time override SLAMGB_GEMM_STAGES): the
+// network's products have 2-12 chunks per output tile, so fewer stages and
+// more resident CTAs per SM hide the load latency better than deep per-CTA
+// pipelines.
+#ifndef SLAMGB_GEMM_STAGES
+#define SLAMGB_GEMM_STAGES 3
+#endif
+template <int BN, class LA, class LB, class EP, bool F16 = false, int S = SLAMGB_GEMM_STAGES>
 cudaError_t launch_umma_gemm_async(const LA &la, const LB &lb, const EP &ep, int M, int N, int K, int *err,
                                    cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
