@@ -30,7 +30,8 @@ NUMERIC = ["--ftz=true", "--prec-div=false", "--prec-sqrt=false"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
 
 # translation units of the tracker library
-CU_SOURCES = ["odo_maps.cu", "odo_track.cu", "depth_filter.cu", "model_predict.cu", "cnn.cu", "synth_gpu.cu"]
+CU_SOURCES = ["odo_maps.cu", "odo_track.cu", "depth_filter.cu", "model_predict.cu", "cnn.cu", "synth_gpu.cu",
+              "transfer.cu"]
 CPP_SOURCES = ["odo_host.cpp", "batch_host.cpp", "cnn_host.cpp", "inputs_host.cpp"]
 
 

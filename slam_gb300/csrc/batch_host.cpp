@@ -79,6 +79,7 @@ struct odo_batch {
     int max_nb[kLevels];
     int max_w = 0, max_h = 0;
     float *init_dev = nullptr;  // [max_pairs][6] warm-start motions (odo_batch_track_init)
+    float *prop_host = nullptr; // pinned copy of the network's proposals (fall-back decisions)
     int last_n = 0, last_rgb = 0;  // pair count and photometric flag of the last tracking call
     bool follow_legacy = true;     // stream NULL: order after the legacy default stream's work
     cudaEvent_t order_ev = nullptr;
@@ -436,8 +437,11 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
 cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, const int max_iters[kLevels],
                           bool prep = true, int live_maps = 0) {
     cudaStream_t s = b->stream;
-    cudaError_t e = cudaMemcpyAsync(b->args_dev, b->args_host, b->args_bytes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_dev, b->st_host, sizeof(TrackState) * n, cudaMemcpyHostToDevice, s);
+    // argument blocks and states travel by a copy kernel over the pinned
+    // host buffers, not queued behind the caller's bulk copies on the copy
+    // engines
+    cudaError_t e = launch_host_copy(b->args_dev, b->args_host, b->args_bytes, s);
+    if (e == cudaSuccess) e = launch_host_copy(b->st_dev, b->st_host, sizeof(TrackState) * n, s);
     auto A = [&](size_t o) { return (const void *)(b->args_dev + o); };
     const int W = b->max_w, Hh = b->max_h;
     if (e == cudaSuccess) e = launch_stamp_batch(b->st_dev, n, s);
@@ -464,7 +468,7 @@ cudaError_t enqueue_batch(odo_batch_t *b, int n, int rgb, int so3, int warm, con
             e = launch_level_iteration_batch((const PassArgs *)A(b->o_pass[l]), n, b->max_nb[l],
                                              rgb ? b->max_nb[l] : 1, b->threads, 0, j, s, 3, b->split_solve);
     if (e == cudaSuccess) e = launch_track_end_batch(b->st_dev, n, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b->st_host, b->st_dev, sizeof(TrackState) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = launch_host_copy(b->st_host, b->st_dev, sizeof(TrackState) * n, s);
     return e;
 }
 
@@ -514,6 +518,8 @@ int odo_batch_create(int max_pairs, odo_batch_t **out) {
     std::memset(b->args_host, 0, o);
     if ((e = cudaMalloc(&b->st_dev, sizeof(TrackState) * np)) != cudaSuccess) return bail(e, "cudaMalloc(states)");
     if ((e = cudaMalloc(&b->init_dev, sizeof(float) * 6 * np)) != cudaSuccess) return bail(e, "cudaMalloc(init)");
+    if ((e = cudaMallocHost(&b->prop_host, sizeof(float) * 6 * np)) != cudaSuccess)
+        return bail(e, "cudaMallocHost(proposals)");
     if ((e = cudaEventCreateWithFlags(&b->order_ev, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&b->warm_ev, cudaEventDisableTiming)) != cudaSuccess)
@@ -536,6 +542,7 @@ int odo_batch_destroy(odo_batch_t *b) {
     if (b->st_dev) cudaFree(b->st_dev);
     if (b->st_host) cudaFreeHost(b->st_host);
     if (b->init_dev) cudaFree(b->init_dev);
+    if (b->prop_host) cudaFreeHost(b->prop_host);
     if (b->order_ev) cudaEventDestroy(b->order_ev);
     if (b->side_stream) {
         cudaStreamSynchronize(b->side_stream);
@@ -754,8 +761,9 @@ int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, 
     if (rc2 != ODO_OK) return rc2;
     // 3. fall-back decisions on the host: residual, and the angle between the
     //    refined rotation and the proposed one, R_prop = R_pose exp(w)
-    std::vector<float> prop((size_t)6 * npairs);
-    BCK(cudaMemcpy(prop.data(), b->init_dev, prop.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    BCK(launch_host_copy(b->prop_host, b->init_dev, sizeof(float) * 6 * npairs, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    const float *prop = b->prop_host;
     std::vector<int> idx;
     for (int i = 0; i < npairs; ++i) {
         bool fb = wp->residual_limit > 0 && !(results[i].lastICPError <= wp->residual_limit);

@@ -16,6 +16,12 @@
 
 using namespace slamgb::cnn;
 
+namespace slamgb {
+// transfer.cu: pinned host <-> device copy by a kernel (not the copy engines)
+cudaError_t launch_host_copy(void *dst, const void *src, size_t bytes, cudaStream_t s);
+}  // namespace slamgb
+using slamgb::launch_host_copy;
+
 struct odo_cnn {
     Net net;
     int device = 0;
@@ -270,7 +276,7 @@ static int pack_input_on(odo_cnn_t *n, const odo_pair *pairs, int npairs, uint16
                                    q.depth,       q.depth_pitch, q.rgba,       q.rgba_pitch,
                                    sc};
     }
-    CCK(cudaMemcpyAsync(n->pack_dev, n->pack_host, sizeof(PackArgs) * npairs, cudaMemcpyHostToDevice, s));
+    CCK(launch_host_copy(n->pack_dev, n->pack_host, sizeof(PackArgs) * npairs, s));
     CCK(cudaEventRecord(n->pack_done, s));
     CCK(cnn_pack(n->pack_dev, npairs, input_dev, s));
     return ODO_OK;
@@ -287,7 +293,7 @@ int cnn_propose_on(odo_cnn_t *n, const odo_pair *pairs, int npairs, float *out_d
         CCK(cnn_forward(N, n->in_buf, m, st));
         CCK(cudaMemcpyAsync(out_dev + (size_t)6 * s, N.out, (size_t)m * kOut * 4, cudaMemcpyDeviceToDevice, st));
     }
-    CCK(cudaMemcpyAsync(n->flag_host, N.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CCK(launch_host_copy(n->flag_host, N.err, sizeof(int), st));
     CCK(cudaEventRecord(n->done, st));
     return ODO_OK;
 }

@@ -231,7 +231,9 @@ void drop_graphs(odo_t *h) {
 // Enqueues one whole tracking call on the stream.
 cudaError_t enqueue_track(odo_t *h, const int iterations[kLevels], int icp, int rgb, int so3) {
     cudaStream_t s = h->stream;
-    cudaError_t e = cudaMemcpyAsync(h->st_dev, h->st_host, sizeof(TrackState), cudaMemcpyHostToDevice, s);
+    // the state travels by a copy kernel (not queued behind the caller's
+    // bulk copies on the copy engines)
+    cudaError_t e = launch_host_copy(h->st_dev, h->st_host, sizeof(TrackState), s);
     if (e != cudaSuccess) return e;
     if (rgb && (e = enqueue_derivatives(h, s)) != cudaSuccess) return e;
     if (so3) {
@@ -258,7 +260,7 @@ cudaError_t enqueue_track(odo_t *h, const int iterations[kLevels], int icp, int 
         }
     }
     if ((e = launch_track_end(h->st_dev, s)) != cudaSuccess) return e;
-    return cudaMemcpyAsync(h->st_host, h->st_dev, sizeof(TrackState), cudaMemcpyDeviceToHost, s);
+    return launch_host_copy(h->st_host, h->st_dev, sizeof(TrackState), s);
 }
 
 int check_handle(odo_t *h) { return h ? ODO_OK : ODO_ERR_ARG; }

@@ -261,4 +261,9 @@ cudaError_t launch_debug_rgb_step(const LevelArgs &L, float sigma, double *out29
 cudaError_t launch_debug_so3(Img<const uint8_t> last, Img<const uint8_t> next, const float *params_dev,
                              double *out11_dev, cudaStream_t s);
 
+// Copy between pinned host memory (addressed by the device directly) and
+// device memory by a kernel on stream s, not by the copy engines
+// (transfer.cu).
+cudaError_t launch_host_copy(void *dst, const void *src, size_t bytes, cudaStream_t s);
+
 }  // namespace slamgb
