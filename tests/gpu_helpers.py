@@ -215,6 +215,14 @@ class OracleRuns:
             out[name] = pose_diff(t32, R32, t, R)
         return out
 
+    def summation_gap(self):
+        """Largest pose change (rad or m) of the oracle's own result under the
+        perturbations that are properties of the reference algorithm rather
+        than of the oracle's IEEE arithmetic: another summation order (the
+        reference's depends on its launch shape) and FP64 arithmetic."""
+        t32, R32, _ = self.run(32)
+        return max(max(pose_diff(t32, R32, *self.run(*PERTURBATIONS[k])[:2])) for k in ("order", "order_b", "fp64"))
+
     def undetermined(self):
         worst = max(max(v) for v in self.sensitivity().values())
         return not np.isfinite(worst) or worst > UNDETERMINED

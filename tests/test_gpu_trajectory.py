@@ -17,8 +17,8 @@ sensitivity)."""
 import numpy as np
 import pytest
 
-from gpu_helpers import (POSE_TOL_M, POSE_TOL_RAD, OracleRuns, check_pose, dev, dev_u16, gpu_images, new_gpu_odo,
-                         pose_diff, report, set_images)
+from gpu_helpers import (GAP_LIMIT, POSE_TOL_M, POSE_TOL_RAD, OracleRuns, check_pose, dev, dev_u16, gpu_images,
+                         new_gpu_odo, pose_diff, report, set_images)
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +35,7 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
     prev = synth.render(scene, T[0], cam, noise_seed=seed * 100003, depth=False, rgba=True)
     g.initFirstRGB(dev(prev["rgba"]))
     est = [T[0].astype(np.float32).astype(np.float64)]
-    rot_err, tr_err, jtj_err, flat_frames = [], [], [], []
+    rot_err, tr_err, jtj_err, flat_frames, determined = [], [], [], [], []
     for k in range(1, FRAMES):
         start = est[-1].astype(np.float32)
         model = synth.render(scene, start.astype(np.float64), cam, depth=False, rgba=True, model=True)
@@ -74,9 +74,11 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
         tr_err.append(tr)
         jtj_err.append(jtj)
         flat_frames.append(flat)
+        determined.append(ref.summation_gap() < GAP_LIMIT)
         est.append(synth.pose(Ro, to))
         prev = live
-    rot_err, tr_err, jtj_err, flat_frames = (np.array(v) for v in (rot_err, tr_err, jtj_err, flat_frames))
+    rot_err, tr_err, jtj_err, flat_frames, determined = (np.array(v) for v in (rot_err, tr_err, jtj_err, flat_frames,
+                                                                                 determined))
     within = float(np.mean(flat_frames))
     jf = jtj_err[flat_frames] if flat_frames.any() else np.zeros(1)
     ate = evaluate.ate_rmse(np.array(T), np.array(est))
@@ -87,3 +89,6 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
            % (FRAMES, rot_err.max(), tr_err.max(), np.percentile(rot_err, 99), np.percentile(tr_err, 99),
               100 * within, jf.max(), np.percentile(jf, 99), jtj_err.max(), np.percentile(jtj_err, 99), ate,
               rpe["trans_rmse"], np.degrees(rpe["rot_rmse"])))
+    report("trajectory: on %d of %d frames the oracle's own pose moves by less than %.0e under another summation "
+           "order and in FP64 (the reference algorithm determines the pose there); the GPU is within the flat 1e-5 "
+           "on %d of them" % (determined.sum(), len(determined), GAP_LIMIT, (determined & flat_frames).sum()))
