@@ -32,6 +32,8 @@ Multi-GPU: replicas (a tracking call does not shard); each rank tracks its own
 copy of the workload; value = frames of all ranks / max time over ranks.
 """
 import argparse
+import contextlib
+import gc
 import json
 import math
 import os
@@ -99,6 +101,22 @@ def parse():
     if a.pairs is None:
         a.pairs = 1000 if a.study == "precision" else 512
     return a
+
+
+@contextlib.contextmanager
+def no_gc():
+    """Python's cyclic garbage collector paused over a timed region (as
+    timeit does): a full collection of the held-out set's Python objects
+    takes tens to hundreds of milliseconds and would be charged to whichever
+    step it falls in.  The library itself allocates nothing per call."""
+    gc.collect()
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
 
 
 def dist_env():
@@ -226,7 +244,8 @@ def run_reference(args):
     cam = synth.Camera()
     frames = [synth.make_pair(args.seed * 31 + 7000 + k, cam=cam, max_deg=10.0, max_m=0.10) for k in range(8)]
     cpu_track(frames, cam, nframes=max(1, args.warmup))
-    n, el = cpu_track(frames, cam, nframes=args.steps)
+    with no_gc():
+        n, el = cpu_track(frames, cam, nframes=args.steps)
     fps = n / el
     out = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / n, "higher_is_better": True,
@@ -286,11 +305,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     poses = []
-    e0.record(stream)
-    for k in range(n_single):
-        poses.append(step(dframes[k % len(dframes)]))
-    e1.record(stream)
-    torch.cuda.synchronize()
+    with no_gc():
+        e0.record(stream)
+        for k in range(n_single):
+            poses.append(step(dframes[k % len(dframes)]))
+        e1.record(stream)
+        torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     if world > 1:
@@ -311,12 +331,13 @@ def run_ours(args):
         odo.set_mode(m)
         for k in range(3):
             step(dframes[k % len(dframes)])
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for k in range(n_single):
-            step(dframes[k % len(dframes)])
-        e1.record(stream)
-        torch.cuda.synchronize()
+        with no_gc():
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for k in range(n_single):
+                step(dframes[k % len(dframes)])
+            e1.record(stream)
+            torch.cuda.synchronize()
         mode_fps[name] = n_single / (e0.elapsed_time(e1) / 1000.0)
     odo.set_mode({"graph": MODE_GRAPH, "stream": MODE_STREAM, "persistent": MODE_PERSISTENT}[args.mode])
     for k in range(3):
@@ -331,14 +352,15 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2.record(stream)
-    for k in range(n_single):
-        h = hframes[k % len(hframes)]
-        for key in ekeys:
-            stage[key].copy_(h[key], non_blocking=True)
-        step({**stage, "T1": h["T1"]})
-    e3.record(stream)
-    torch.cuda.synchronize()
+    with no_gc():
+        e2.record(stream)
+        for k in range(n_single):
+            h = hframes[k % len(hframes)]
+            for key in ekeys:
+                stage[key].copy_(h[key], non_blocking=True)
+            step({**stage, "T1": h["T1"]})
+        e3.record(stream)
+        torch.cuda.synchronize()
     ms_e2e = e2.elapsed_time(e3)
     if world > 1:
         tt = torch.tensor([ms_e2e], device="cuda")
@@ -622,12 +644,13 @@ def measure_warm_batched(args, stream, local, world):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def timed(fn, steps):
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for k in range(steps):
-            fn(k)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        with no_gc():
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for k in range(steps):
+                fn(k)
+            e1.record(stream)
+            torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
     # ---- warm-started, inputs resident in HBM: exactly K steps ----
@@ -711,23 +734,24 @@ def measure_warm_batched(args, stream, local, world):
     h2d_gbs = batch_bytes / t_h2d / 1e9
     for ev in ev_used:
         ev.record(stream)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for c in css:
-        c.wait_event(e0)
-    issue_copy(0)
     step_host = []
-    for k in range(K):
-        th = time.perf_counter()
-        if k + 1 < K:
-            issue_copy(k + 1)
-        for ev in ev_copy[k % nh]:
-            stream.wait_event(ev)
-        _, fb_k = b.track_warm(net, fps[k % nh], descs=descs[k % nh], **tuned)
-        ev_used[k % nh].record(stream)
-        step_host.append([round((time.perf_counter() - th) * 1e3, 2), int(fb_k.sum())])
-    e1.record(stream)
-    torch.cuda.synchronize()
+    with no_gc():
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for c in css:
+            c.wait_event(e0)
+        issue_copy(0)
+        for k in range(K):
+            th = time.perf_counter()
+            if k + 1 < K:
+                issue_copy(k + 1)
+            for ev in ev_copy[k % nh]:
+                stream.wait_event(ev)
+            _, fb_k = b.track_warm(net, fps[k % nh], descs=descs[k % nh], **tuned)
+            ev_used[k % nh].record(stream)
+            step_host.append([round((time.perf_counter() - th) * 1e3, 2), int(fb_k.sum())])
+        e1.record(stream)
+        torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1)
     if world > 1:
         tt = torch.tensor([ms_e2e], device="cuda")
@@ -821,12 +845,13 @@ def measure_batched_verification(args, stream, world):
         b.track(fps, descs=descs)
     K = max(args.steps, 3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(K):
-        res = b.track(fps, descs=descs)
-    e1.record(stream)
-    torch.cuda.synchronize()
+    with no_gc():
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(K):
+            res = b.track(fps, descs=descs)
+        e1.record(stream)
+        torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / K
     if world > 1:
         tt = torch.tensor([ms], device="cuda")
