@@ -741,17 +741,25 @@ def measure_warm_batched(args, stream, local, world):
         for c in css:
             c.wait_event(e0)
         issue_copy(0)
+        ev_in = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        ev_out = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
         for k in range(K):
             th = time.perf_counter()
             if k + 1 < K:
                 issue_copy(k + 1)
             for ev in ev_copy[k % nh]:
                 stream.wait_event(ev)
+            ev_in[k].record(stream)
+            th2 = time.perf_counter()
             _, fb_k = b.track_warm(net, fps[k % nh], descs=descs[k % nh], **tuned)
+            ev_out[k].record(stream)
             ev_used[k % nh].record(stream)
-            step_host.append([round((time.perf_counter() - th) * 1e3, 2), int(fb_k.sum())])
+            step_host.append([round((time.perf_counter() - th) * 1e3, 2), round((time.perf_counter() - th2) * 1e3, 2),
+                              int(fb_k.sum())])
         e1.record(stream)
         torch.cuda.synchronize()
+        for k in range(K):  # device time from the step's inputs being in place to the end of its tracking
+            step_host[k].append(round(ev_in[k].elapsed_time(ev_out[k]), 2))
     ms_e2e = e0.elapsed_time(e1)
     if world > 1:
         tt = torch.tensor([ms_e2e], device="cuda")
@@ -789,7 +797,7 @@ def measure_warm_batched(args, stream, local, world):
             "e2e": {"value": K * nb / (ms_e2e * 1e-3), "unit": "frames/s", "h2d_bytes_per_step": int(batch_bytes),
                     "d2h_bytes_per_step": int(nb * ctypes_sizeof_result()), "h2d_gbs_alone": h2d_gbs,
                     "note": "copies of step k+1 (4 copy streams) overlap the tracking of step k (two input buffers)",
-                    "step_host_ms_and_fallbacks": step_host},
+                    "steps_host_ms_track_host_ms_fallbacks_track_device_ms": step_host},
             "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres_b (level 0, all pairs of a step)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "alg_bytes_per_px": BYTES_PER_PX_ITER,
