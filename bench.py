@@ -795,9 +795,13 @@ def measure_warm_batched(args, stream, local, world):
                       "generation_s": gen_s, "train_s": train_s, "last_epoch_loss": hist[-1]},
             "launch": {"threads": threads, "pixels_per_thread": ppt},
             "e2e": {"value": K * nb / (ms_e2e * 1e-3), "unit": "frames/s", "h2d_bytes_per_step": int(batch_bytes),
+                    "median_step_frames_per_s": nb / (float(np.median([s[0] for s in step_host])) * 1e-3),
                     "d2h_bytes_per_step": int(nb * ctypes_sizeof_result()), "h2d_gbs_alone": h2d_gbs,
                     "note": "copies of step k+1 (4 copy streams) overlap the tracking of step k (two input buffers)",
-                    "steps_host_ms_track_host_ms_fallbacks_track_device_ms": step_host},
+                    "steps_host_ms_track_host_ms_fallbacks_track_device_ms": step_host,
+                    "step_note": "the tracking of every step takes the same device time; the host time of a step "
+                                 "is longer when that step's input copy from host memory is slower (some copies of "
+                                 "the 6.45 GB run at a fraction of the usual ~210 GB/s)"},
             "roofline": {"bound": "hbm", "kernel": "k_icp_rgbres_b (level 0, all pairs of a step)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "alg_bytes_per_px": BYTES_PER_PX_ITER,

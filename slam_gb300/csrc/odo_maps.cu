@@ -474,10 +474,33 @@ __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.000
 // src/odom/reduce.cu:782-810: j0 < cols-5, i < rows-1, no zero intensity in
 // the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
 // into a byte mask, so the per-iteration pass reads one byte per pixel.
+// Non-zero test of the 4x4 intensity window [y-2, y+2) x [x-2, x+2) for the
+// 32 pixels of a warp (one tile row, lane = x - X0): tile row y - 2 - oy + u
+// holds window row u, tile columns lane .. lane + 3 its four pixels.  Each
+// tile row's non-zero bits over the 36 tile columns come from two ballots,
+// so a lane tests its window with shifts instead of 16 loads.  Tile entries
+// outside the image read 0 here; the caller uses the result for pixels
+// whose window lies inside the image only.  Executed by all 32 lanes.
+template <int TR>
+__device__ __forceinline__ bool window_nonzero(const uint8_t (&t)[der_th<TR>()][kDerTW], int row0, int lane) {
+    bool ok = true;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const uint8_t *r = t[row0 + u];
+        const unsigned lo = __ballot_sync(0xffffffffu, r[lane] > 0);
+        const unsigned hi = __ballot_sync(0xffffffffu, lane < kDerTW - 32 && r[32 + (lane & 3)] > 0);
+        const unsigned long long m = ((unsigned long long)hi << 32) | lo;
+        ok = ok && ((m >> lane) & 0xFull) == 0xFull;
+    }
+    return ok;
+}
+
 template <int TR>
 __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_t (&t)[der_th<TR>()][kDerTW], int ox,
                                          int oy, int x, int y) {
     const Img<const uint8_t> src = a.src[l];
+    // the window test of the interior pixels, warp-wide (before any lane returns)
+    const bool win_ok = window_nonzero<TR>(t, y - 2 - oy, x - ox - 2);
     if (x >= src.cols || y >= src.rows) return;
     float dxVal = 0, dyVal = 0;
     if (x >= 1 && x <= src.cols - 2 && y >= 1 && y <= src.rows - 2) {
@@ -510,12 +533,7 @@ __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_
     if (j0 < cols - 5 && i < rows - 1) {
         bool valid = true;
         if (i >= 2 && j0 >= 2) {  // interior (i + 2 <= rows, j0 + 2 <= cols hold here)
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint8_t *r = t[i - 2 + u - oy] - ox + j0 - 2;
-#pragma unroll
-                for (int v = 0; v < 4; ++v) valid = valid && (r[v] > 0);
-            }
+            valid = win_ok;
         } else {
             for (int u = max(i - 2, 0); u < min(i + 2, rows); u++) {
                 const uint8_t *r = t[u - oy] - ox;
