@@ -63,6 +63,23 @@ __device__ __forceinline__ void tile_origin(const LevelTiles &t, int b, int &l, 
 // [Y0 - 2, Y0 + TR + 1).  Tile entries outside the image are never read
 // (the loops clamp to the image).
 constexpr int kDownTW = 2 * BX + 4, kDerTW = BX + 4;
+
+// The batched kernels read their pair's argument block from a device array.
+// Read there directly, every field would be re-loaded from global memory
+// after each global store of the kernel (the compiler cannot rule out that a
+// store changes it); a copy in shared memory (which global stores cannot
+// touch) is loaded once.  All threads of the block take part.
+template <typename T>
+__device__ __forceinline__ const T &stage_args(T &dst, const T &src) {
+    static_assert(sizeof(T) % 4 == 0, "word copy");
+    unsigned *d = reinterpret_cast<unsigned *>(&dst);
+    const unsigned *s = reinterpret_cast<const unsigned *>(&src);
+    const int tid = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    for (int k = tid; k < (int)(sizeof(T) / 4); k += nt) d[k] = s[k];
+    __syncthreads();
+    return dst;
+}
 template <int TR>
 __host__ __device__ constexpr int down_th() { return 2 * TR + 4; }
 template <int TR>
@@ -153,7 +170,8 @@ __global__ void k_pyr_down_depth(PyrArgs a) {
     pyr_tile<kTileRowsSingle>(a, blockIdx.x * BX, blockIdx.y * kTileRowsSingle);
 }
 __global__ void k_pyr_down_depth_b(const PyrArgs *A) {
-    pyr_tile<kTileRowsBatch>(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
+    __shared__ PyrArgs sa;
+    pyr_tile<kTileRowsBatch>(stage_args(sa, A[blockIdx.z]), blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
 }
 
 // computeVmapKernel, src/odom/utils.cu:109-133, for one pixel.
@@ -199,7 +217,10 @@ __device__ __forceinline__ void vnmap_tile(const VNArgs &a, const LevelTiles &t)
     for (int r = 0; r < t.th / BY; ++r) vnmap_px(a, l, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
 __global__ void k_vmap_nmap(VNArgs a, LevelTiles t) { vnmap_tile(a, t); }
-__global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) { vnmap_tile(A[blockIdx.z], t); }
+__global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) {
+    __shared__ VNArgs sa;
+    vnmap_tile(stage_args(sa, A[blockIdx.z]), t);
+}
 
 // copyMapsKernel (src/odom/utils.cu:270-310): a pixel is valid iff the
 // vertex z != 0.
@@ -299,7 +320,10 @@ __device__ __forceinline__ void model_tile(const ModelArgs &a, int tile) {
         store_model_px(a, vm2, nm2, X2, Y2, resize4<false>(v1, v1x, v1y, v1xy), resize4<true>(n1, n1x, n1y, n1xy));
 }
 __global__ void __launch_bounds__(256) k_model_maps(ModelArgs a) { model_tile(a, blockIdx.x); }
-__global__ void __launch_bounds__(256) k_model_maps_b(const ModelArgs *A) { model_tile(A[blockIdx.z], blockIdx.x); }
+__global__ void __launch_bounds__(256) k_model_maps_b(const ModelArgs *A) {
+    __shared__ ModelArgs sa;
+    model_tile(stage_args(sa, A[blockIdx.z]), blockIdx.x);
+}
 
 // verticesToDepthKernel (src/odom/utils.cu:526-537, cut at maxDepthRGB =
 // 6.0, src/odom/RGBDOdometryef.cpp:37) and bgr2IntensityKernel
@@ -352,7 +376,9 @@ __global__ void k_rgbd_level0(RgbdArgs a) {
     rgbd_px4(a, 4 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y * blockDim.y + threadIdx.y);
 }
 __global__ void k_rgbd_level0_b(const RgbdArgs *A) {
-    rgbd_px4(A[blockIdx.z], 4 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y * blockDim.y + threadIdx.y);
+    __shared__ RgbdArgs sa;
+    rgbd_px4(stage_args(sa, A[blockIdx.z]), 4 * (blockIdx.x * blockDim.x + threadIdx.x),
+             blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 __constant__ float c_gauss5x5[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36, 24, 6, 4, 16, 24, 16, 4, 1, 4, 6, 4, 1};
@@ -460,7 +486,8 @@ __global__ void k_gauss_down(GaussArgs a) {
     gauss_tile<kTileRowsSingle>(a, blockIdx.x * BX, blockIdx.y * kTileRowsSingle);
 }
 __global__ void k_gauss_down_b(const GaussArgs *A) {
-    gauss_tile<kTileRowsBatch>(A[blockIdx.z], blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
+    __shared__ GaussArgs sa;
+    gauss_tile<kTileRowsBatch>(stage_args(sa, A[blockIdx.z]), blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
 }
 
 __constant__ float c_sobel_x[9] = {0.52201f, 0.00000f, -0.52201f, 0.79451f, -0.00000f,
@@ -559,7 +586,10 @@ __device__ __forceinline__ void deriv_tile(const DerivArgs &a, const LevelTiles 
     for (int r = 0; r < TR / BY; ++r) deriv_px<TR>(a, l, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
 __global__ void k_derivatives(DerivArgs a, LevelTiles t) { deriv_tile<kTileRowsSingle>(a, t); }
-__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) { deriv_tile<kTileRowsBatch>(A[blockIdx.z], t); }
+__global__ void k_derivatives_b(const DerivArgs *A, LevelTiles t) {
+    __shared__ DerivArgs sa;
+    deriv_tile<kTileRowsBatch>(stage_args(sa, A[blockIdx.z]), t);
+}
 
 inline dim3 grid2(int cols, int rows, int z = 1) { return dim3((cols + BX - 1) / BX, (rows + BY - 1) / BY, z); }
 // grid of the window kernels: 32 x th outputs per block
