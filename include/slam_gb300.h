@@ -479,6 +479,14 @@ typedef struct {
 int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, int npairs,
                          const odo_warm_params *wp, odo_pair_result *results, int *fallback);
 
+/* Copies `bytes` between pinned host memory (cudaMallocHost / cudaHostAlloc
+ * / pinned tensors: the device addresses it directly) and device memory, in
+ * either direction, by a kernel on `stream` instead of the copy engines --
+ * the way the tracker moves its own argument blocks and states, so that it
+ * never waits behind a caller's bulk copies; callers may use it for their
+ * frames too.  Asynchronous; ODO_ERR_ARG on NULL pointers. */
+int odo_host_copy(void *dst, const void *src, size_t bytes, void *stream);
+
 /* PNG scanline filter reconstruction (filter types 0-4 of the PNG format)
  * for the TUM-format frame reader, whose reference reads its PNG images
  * through OpenCV (src/inputs/FileReader.cpp:43-55): `filtered` holds
@@ -503,9 +511,10 @@ int odo_synth_render(const void *scenes_host, int nscenes, const int *view_scene
  * self-check of the layout) or 2 (layout 0 with FP16 operands), plus 4 for
  * the failure-detection test of the bounded tensor-core waits (one wait
  * runs out on a barrier that nothing arrives at; returns ODO_ERR_TIMEOUT
- * after draining the issued MMAs; needs K > 128); layout = 8: the kernel
- * the network's forward pass uses (operands copied into shared memory by
- * cp.async, a few K chunks in flight), BF16, library layout. */
+ * after draining the issued MMAs; needs K > 128); layout = 8: the
+ * asynchronously fed kernel (operands copied into shared memory by
+ * cp.async, a few K chunks in flight), BF16; layout = 9: the same with B
+ * loaded by TMA, as the network's forward pass runs it (K a multiple of 8). */
 int odo_cnn_debug_gemm(const uint16_t *A_dev, const uint16_t *B_dev, float *C_dev, int M, int N, int K, int bn,
                        int layout, void *stream);
 

@@ -107,6 +107,7 @@ SIGNATURES = [
                             c_int, c_int, c_float, c_float, c_float, c_float, c_int, c_void_p, c_void_p, c_size_t,
                             c_void_p, c_size_t, c_void_p]),
     ("odo_png_unfilter", c_int, [c_void_p, c_int, c_size_t, c_int, c_void_p]),
+    ("odo_host_copy", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
     ("odo_filter_depth", c_int, [c_void_p, c_size_t, c_void_p, c_size_t, c_int, c_int, c_float, c_void_p]),
     ("odo_depth_metric", c_int, [c_void_p, c_size_t, c_void_p, c_size_t, c_int, c_int, c_float, c_void_p]),
     ("odo_init_icp_model", c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_float, P(c_float)]),

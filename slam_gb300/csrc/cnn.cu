@@ -466,13 +466,51 @@ cudaError_t gemm(const LA &a, const LB &b, const EP &e, int M, int N, int K, int
     return launch_umma_gemm<128, LA, LB, EP, F16>(a, b, e, M, N, K, splits, 0, err, s);
 }
 
-// Forward products: operands copied into shared memory by cp.async, a few
-// K chunks in flight per CTA (k_umma_gemm_async).
+// Forward products (k_umma_gemm_async): the activations' implicit im2col
+// rows copied into shared memory by cp.async, the weights by TMA, a few K
+// chunks in flight per CTA.
+inline int gemm_bn(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : 128); }
 template <bool F16 = false, class LA, class LB, class EP>
-cudaError_t gemm_async(const LA &a, const LB &b, const EP &e, int M, int N, int K, int *err, cudaStream_t s) {
-    if (N <= 32) return launch_umma_gemm_async<32, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);
-    if (N <= 64) return launch_umma_gemm_async<64, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);
-    return launch_umma_gemm_async<128, LA, LB, EP, F16>(a, b, e, M, N, K, err, s);
+cudaError_t gemm_async(const LA &a, const LB &b, const EP &e, int M, int N, int K, int *err, cudaStream_t s,
+                       const CUtensorMap *tmb = nullptr) {
+    if (N <= 32) return launch_umma_gemm_async<32, LA, LB, EP, F16>(a, b, e, M, N, K, err, s, tmb);
+    if (N <= 64) return launch_umma_gemm_async<64, LA, LB, EP, F16>(a, b, e, M, N, K, err, s, tmb);
+    return launch_umma_gemm_async<128, LA, LB, EP, F16>(a, b, e, M, N, K, err, s, tmb);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// TMA descriptor of a row-major 16-bit weight matrix [N][K] (K % 8 == 0,
+// 16-byte aligned rows): boxes of box_rows (default gemm_bn(N)) rows x 8 K
+// values, zero fill outside the matrix.
+bool weight_map(CUtensorMap *m, const uint16_t *w, int N, int K, int box_rows = 0) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn || (K % 8) != 0 || (reinterpret_cast<uintptr_t>(w) & 15) != 0) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)N};
+    const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)(box_rows > 0 ? box_rows : gemm_bn(N))};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<uint16_t *>(w), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
@@ -485,21 +523,30 @@ cudaError_t gemm_async(const LA &a, const LB &b, const EP &e, int M, int N, int 
 
 cudaError_t cnn_forward(Net &n, const uint16_t *input, int B, cudaStream_t s) {
     const ParamLayout &P = n.L;
+    const int l1 = kConv, l2 = kConv + 1;
+    if (n.tm_state == 0) {  // the weights never move: their TMA descriptors are built once
+        bool ok = weight_map(&n.tmw[0], n.wh, kCout[0], w_cols(0));
+        for (int l = 1; l < kConv && ok; ++l) ok = weight_map(&n.tmw[l], n.wbf + P.w[l], kCout[l], w_cols(l));
+        ok = ok && weight_map(&n.tmw[l1], n.wbf + P.w[l1], kHidden, kFlat);
+        ok = ok && weight_map(&n.tmw[l2], n.wbf + P.w[l2], kOut, kHidden);
+        n.tm_state = ok ? 1 : -1;
+    }
+    auto tm = [&](int l) { return n.tm_state == 1 ? &n.tmw[l] : nullptr; };
     for (int l = 0; l < kConv; ++l) {
         const ConvGeo g = conv_geo(l, B);
         const int M = B * g.Ho * g.Wo, N = kCout[l], K = w_cols(l);
         const EpBiasAct ep{n.act[l + 1], n.master + P.b[l], N, N, 1};
         // the first layer in FP16 (the FP16 depth keeps 11 significant bits)
         if (l == 0)
-            CNN_CK(gemm_async<true>(LdIm2col<false>{input, g}, LdDense{n.wh, N, K, K}, ep, M, N, K, n.err, s));
+            CNN_CK(gemm_async<true>(LdIm2col<false>{input, g}, LdDense{n.wh, N, K, K}, ep, M, N, K, n.err, s, tm(0)));
         else
-            CNN_CK(gemm_async(LdIm2col<false>{n.act[l], g}, LdDense{n.wbf + P.w[l], N, K, K}, ep, M, N, K, n.err, s));
+            CNN_CK(gemm_async(LdIm2col<false>{n.act[l], g}, LdDense{n.wbf + P.w[l], N, K, K}, ep, M, N, K, n.err, s,
+                              tm(l)));
     }
-    const int l1 = kConv, l2 = kConv + 1;
     CNN_CK(gemm_async(LdDense{n.act[kConv], B, kFlat, kFlat}, LdDense{n.wbf + P.w[l1], kHidden, kFlat, kFlat},
-                      EpBiasAct{n.hid, n.master + P.b[l1], kHidden, kHidden, 1}, B, kHidden, kFlat, n.err, s));
+                      EpBiasAct{n.hid, n.master + P.b[l1], kHidden, kHidden, 1}, B, kHidden, kFlat, n.err, s, tm(l1)));
     CNN_CK(gemm_async(LdDense{n.hid, B, kHidden, kHidden}, LdDense{n.wbf + P.w[l2], kOut, kHidden, kHidden},
-                      EpBiasF32{n.out, n.master + P.b[l2], kOut, kOut}, B, kOut, kHidden, n.err, s));
+                      EpBiasF32{n.out, n.master + P.b[l2], kOut, kOut}, B, kOut, kHidden, n.err, s, tm(l2)));
     return cudaSuccess;
 }
 
@@ -587,11 +634,17 @@ cudaError_t cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M
                            int *err, cudaStream_t s) {
     const LdDense la{A, M, K, (K + 7) & ~7}, lb{B, N, K, (K + 7) & ~7};
     const EpStore ep{C, N, N};
-    if (layout == 8) {  // the asynchronously fed kernel (BF16)
-        if (bn == 32) return launch_umma_gemm_async<32>(la, lb, ep, M, N, K, err, s);
-        if (bn == 64) return launch_umma_gemm_async<64>(la, lb, ep, M, N, K, err, s);
-        if (bn == 128) return launch_umma_gemm_async<128>(la, lb, ep, M, N, K, err, s);
-        return launch_umma_gemm_async<256>(la, lb, ep, M, N, K, err, s);
+    if (layout == 8 || layout == 9) {  // the asynchronously fed kernel (BF16); 9: B by TMA
+        CUtensorMap map;
+        const CUtensorMap *tmb = nullptr;
+        if (layout == 9) {
+            if (!weight_map(&map, B, N, K, bn)) return cudaErrorNotSupported;
+            tmb = &map;
+        }
+        if (bn == 32) return launch_umma_gemm_async<32>(la, lb, ep, M, N, K, err, s, tmb);
+        if (bn == 64) return launch_umma_gemm_async<64>(la, lb, ep, M, N, K, err, s, tmb);
+        if (bn == 128) return launch_umma_gemm_async<128>(la, lb, ep, M, N, K, err, s, tmb);
+        return launch_umma_gemm_async<256>(la, lb, ep, M, N, K, err, s, tmb);
     }
     if ((layout & 3) == 2) {  // FP16 operands
         const int lay = layout & 4;

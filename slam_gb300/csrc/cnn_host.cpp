@@ -346,7 +346,7 @@ int odo_cnn_train_step(odo_cnn_t *n, const uint16_t *input, const float *labels,
 
 int odo_cnn_debug_gemm(const uint16_t *A, const uint16_t *B, float *C, int M, int N, int K, int bn, int layout,
                        void *stream) {
-    if (!A || !B || !C || M < 1 || N < 1 || K < 1 || (layout & 3) > 2 || layout < 0 || (layout > 6 && layout != 8))
+    if (!A || !B || !C || M < 1 || N < 1 || K < 1 || (layout & 3) > 2 || layout < 0 || (layout > 6 && layout != 8 && layout != 9))
         return ODO_ERR_ARG;
     if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return ODO_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;

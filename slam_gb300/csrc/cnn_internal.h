@@ -11,6 +11,7 @@
 // Weights are stored [out][in] with the conv input index (ky * 3 + kx) * Cin + ci;
 // activations are BF16 NHWC after the ReLU, the output FP32.
 #pragma once
+#include <cuda.h>
 #include <cstddef>
 #include <cstdint>
 
@@ -81,6 +82,10 @@ struct Net {
     float *metric = nullptr;      // loss metric, 6x6 row-major
     int *err = nullptr;           // tensor-core wait time-out flag
     int step = 0;
+    // TMA descriptors of the forward weights ([N][K] BF16 / FP16, boxes of
+    // BN rows x 8 K values): 0 not built yet, 1 built, -1 unavailable
+    CUtensorMap tmw[kLayers];
+    int tm_state = 0;
 };
 
 // One frame pair's inputs for the network input packer: level-0 images of

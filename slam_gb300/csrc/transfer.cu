@@ -10,6 +10,7 @@
 
 #include <cstdint>
 
+#include "../../include/slam_gb300.h"
 #include "odo_internal.h"
 
 namespace slamgb {
@@ -42,3 +43,8 @@ cudaError_t launch_host_copy(void *dst, const void *src, size_t bytes, cudaStrea
 }
 
 }  // namespace slamgb
+
+extern "C" int odo_host_copy(void *dst, const void *src, size_t bytes, void *stream) {
+    if (!dst || !src) return ODO_ERR_ARG;
+    return slamgb::launch_host_copy(dst, src, bytes, (cudaStream_t)stream) == cudaSuccess ? ODO_OK : ODO_ERR_CUDA;
+}

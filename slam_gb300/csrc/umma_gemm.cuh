@@ -19,6 +19,8 @@
 // Every thread stages a fixed K group of 8 A rows (and BN / 16 B rows).
 // Epilogue: __device__ void operator()(int m, int n0, const float (&v)[8]) const
 #pragma once
+#include <cuda.h>
+
 #include <cstdint>
 
 #include "umma.cuh"
@@ -172,15 +174,39 @@ __device__ __forceinline__ void cp_async_wait_groups() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <int BN, bool F16, int S, class LA, class LB, class EP>
+// TMA (cp.async.bulk.tensor) load of one 2D box into shared memory,
+// completing `bytes` on the mbarrier's transaction count.
+__device__ __forceinline__ void tma_load_2d(void *smem, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            umma::smem_u32(smem)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(umma::smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(umma::smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// TMAB: the B operand (the weights, a dense [N][K] matrix) comes by TMA
+// instead: per stage one thread issues eight boxes of BN rows x 8 K values
+// (16 bytes), K group j landing at j * BN * 16 bytes, so the core matrices
+// of B are 128 bytes apart along N and BN * 16 bytes apart along K; the
+// stage's "full" mbarrier counts the bytes in and the MMA issuer waits on
+// it.  A (the implicit im2col rows) stays on cp.async.
+template <int BN, bool F16, int S, bool TMAB, class LA, class LB, class EP>
 __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, EP ep, int M, int N, int kchunks,
-                                                                  int chunks_per_split, int *err) {
+                                                                  int chunks_per_split, int *err,
+                                                                  const __grid_constant__ CUtensorMap tmb) {
     static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "BN");
     static_assert(S >= 2 && S <= 6, "stages");
     constexpr int A_BYTES = 128 * kGemmKChunk * 2, B_BYTES = BN * kGemmKChunk * 2, STAGE = A_BYTES + B_BYTES;
     constexpr uint32_t IDESC = F16 ? umma::idesc_f16_f32(128, BN) : umma::idesc_bf16_f32(128, BN);
+    // B's core-matrix offsets: along K, along N
+    constexpr uint32_t B_LBO = TMAB ? BN * 16u : 128u, B_SBO = TMAB ? 128u : 1024u;
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t mbar[S];
+    __shared__ __align__(8) uint64_t full[S];
     __shared__ uint32_t tmem_base;
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -195,7 +221,10 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
     }
     if (tid == 0) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) umma::mbar_init(&mbar[s], 1);
+        for (int s = 0; s < S; ++s) {
+            umma::mbar_init(&mbar[s], 1);
+            umma::mbar_init(&full[s], 1);
+        }
         umma::mbar_fence_init();
     }
     umma::fence_before_sync();
@@ -206,11 +235,13 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
     constexpr int AR = 8, BR = BN / 16;
     const int kg = (tid >> 3) & 7;
     typename LA::Row ra[AR];
-    typename LB::Row rb[BR];
 #pragma unroll
     for (int j = 0; j < AR; ++j) ra[j] = la.row(m0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
+    typename LB::Row rb[TMAB ? 1 : BR];
+    if constexpr (!TMAB) {
 #pragma unroll
-    for (int j = 0; j < BR; ++j) rb[j] = lb.row(n0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
+        for (int j = 0; j < BR; ++j) rb[j] = lb.row(n0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
+    }
     auto issue = [&](int c) {
         uint8_t *sa = smem + (c % S) * STAGE;
         uint8_t *sb = sa + A_BYTES;
@@ -222,17 +253,31 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
             const void *g = la.src(ra[j], ca, bytes);
             cp_async16(sa + (tid + 128 * j) * 16, g, bytes);
         }
-        const typename LB::Col cb = lb.col(k8);
+        if constexpr (TMAB) {
+            if (tid == 0) {
+                uint64_t *bar = &full[c % S];
+                mbar_expect_tx(bar, (uint32_t)B_BYTES);
+                const int kx = (c_begin + c) * kGemmKChunk;
 #pragma unroll
-        for (int j = 0; j < BR; ++j) {
-            int bytes;
-            const void *g = lb.src(rb[j], cb, bytes);
-            cp_async16(sb + (tid + 128 * j) * 16, g, bytes);
+                for (int j = 0; j < kGemmKChunk / 8; ++j) tma_load_2d(sb + j * BN * 16, &tmb, kx + 8 * j, n0, bar);
+            }
+        } else {
+            const typename LB::Col cb = lb.col(k8);
+#pragma unroll
+            for (int j = 0; j < BR; ++j) {
+                int bytes;
+                const void *g = lb.src(rb[j], cb, bytes);
+                cp_async16(sb + (tid + 128 * j) * 16, g, bytes);
+            }
         }
     };
+    int issued = 0;  // chunks whose loads were issued
 #pragma unroll
     for (int p = 0; p < S - 1; ++p) {
-        if (p < nch) issue(p);
+        if (p < nch) {
+            issue(p);
+            issued = p + 1;
+        }
         cp_async_group();
     }
     bool ok = true;
@@ -247,22 +292,32 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
                 if (!__syncthreads_and(ok)) break;
             }
             issue(pf);
+            issued = pf + 1;
         }
         cp_async_group();
         cp_async_wait_groups<S - 1>();  // this thread's copies of chunk c have landed
         umma::fence_smem_to_async();
-        __syncthreads();
+        bool bok = true;
+        if (TMAB && tid == 0) bok = umma::mbar_wait(&full[s], (c / S) & 1, kGemmWaitPolls);
+        if (!__syncthreads_and(bok)) {
+            ok = false;
+            break;
+        }
         if (tid == 0) {
             umma::fence_after_sync();
             const uint32_t a0 = umma::smem_u32(smem + s * STAGE), b0 = a0 + A_BYTES;
 #pragma unroll
             for (int k = 0; k < kGemmKChunk / 16; ++k)
                 umma::mma_bf16(tmem, umma::smem_desc(a0 + k * 256, 128u, 1024u),
-                               umma::smem_desc(b0 + k * 256, 128u, 1024u), IDESC, (c > 0 || k > 0) ? 1u : 0u);
+                               umma::smem_desc(b0 + k * 2 * B_LBO, B_LBO, B_SBO), IDESC, (c > 0 || k > 0) ? 1u : 0u);
             umma::mma_commit(&mbar[s]);
         }
     }
     cp_async_wait_groups<0>();
+    // TMA boxes still in flight (a loop left early): wait for them (bounded)
+    // before the CTA's shared memory can go away
+    if (TMAB && tid == 0)
+        for (int q = c; q < issued; ++q) umma::mbar_wait(&full[q % S], (q / S) & 1, kGemmWaitPolls);
     bool drained = true;
     if (c > 0) {
         const int last = c - 1;
@@ -296,20 +351,33 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
 #endif
 template <int BN, class LA, class LB, class EP, bool F16 = false, int S = SLAMGB_GEMM_STAGES>
 cudaError_t launch_umma_gemm_async(const LA &la, const LB &lb, const EP &ep, int M, int N, int K, int *err,
-                                   cudaStream_t s) {
+                                   cudaStream_t s, const CUtensorMap *tmb = nullptr) {
     if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
     const int kchunks = (K + kGemmKChunk - 1) / kGemmKChunk;
     constexpr int smem = gemm_async_smem_bytes<BN, S>();
-    static bool attr_set = false;  // per instantiation
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_async<BN, F16, S, LA, LB, EP>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
     dim3 grid((M + 127) / 128, (N + BN - 1) / BN, 1);
-    k_umma_gemm_async<BN, F16, S, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, kchunks,
-                                                                              err);
+    if (tmb) {
+        static bool attr_set = false;  // per instantiation
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_async<BN, F16, S, true, LA, LB, EP>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+        k_umma_gemm_async<BN, F16, S, true, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks,
+                                                                                        kchunks, err, *tmb);
+    } else {
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_async<BN, F16, S, false, LA, LB, EP>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+        CUtensorMap none{};
+        k_umma_gemm_async<BN, F16, S, false, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks,
+                                                                                         kchunks, err, none);
+    }
     return cudaGetLastError();
 }
 

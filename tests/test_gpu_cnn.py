@@ -34,11 +34,12 @@ def test_umma_gemm_matches_torch(gpu, bn, shape):
     err = (C - ref).abs().max().item()
     tol = 1e-5 * K ** 0.5 * ref.abs().max().item() + 1e-4
     assert err <= tol, (bn, shape, err, tol)
-    # the asynchronously fed kernel of the forward pass: the same MMAs on the
-    # same shared-memory tiles, so the same bits
-    Ca = debug_gemm(A, B, bn=bn, layout=8)
-    torch.cuda.synchronize()
-    assert torch.equal(Ca, C), (bn, shape, (Ca - C).abs().max().item())
+    # the asynchronously fed kernels (B by cp.async, and by TMA as the forward
+    # pass runs it): the same MMAs on the same operand values, so the same bits
+    for layout in (8, 9):
+        Ca = debug_gemm(A, B, bn=bn, layout=layout)
+        torch.cuda.synchronize()
+        assert torch.equal(Ca, C), (bn, shape, layout, (Ca - C).abs().max().item())
 
 
 @pytest.mark.parametrize("bn", [32, 128])
