@@ -782,20 +782,20 @@ def measure_warm_batched(args, stream, local, world):
     warm_graph = 13 + 3 * sum(its[:args.warm_levels])
     plain_graph = 14 + 1 + 3 * 19
     launches = K * (gemm + warm_graph + (plain_graph if fbr > 0 else 0))
-    return {"fps": K * nb / (ms_w * 1e-3), "ms_per_step": ms_w / K, "steps": K, "warmup": W, "batch_pairs": nb,
+    return {"fps": world * K * nb / (ms_w * 1e-3), "ms_per_step": ms_w / K, "steps": K, "warmup": W, "batch_pairs": nb,
             "eval_pairs": nbatch * nb, "pool_batches": nbatch, "batch_bytes": batch_bytes,
             "schedule": {"levels": args.warm_levels, "iterations": list(its), "so3": False},
             "fallback_cfg": {"residual_limit": tuned["residual_limit"], "residual_ratio": args.residual_ratio,
                              "plain_residual_median": plain_res, "max_disagree_deg": args.max_disagree},
             "eval_thresholds": {"residual_ratio": 1.5, "max_disagree_deg": 0.5,
-                                "frames_per_s": nbatch * nb / (ms_s * 1e-3), "ms_per_step": ms_s / nbatch,
+                                "frames_per_s": world * nbatch * nb / (ms_s * 1e-3), "ms_per_step": ms_s / nbatch,
                                 "speedup_vs_plain_batched": (nbatch * nb / (ms_s * 1e-3)) / (K * nb / (ms_p * 1e-3)),
                                 "iterations_saved": saved(acc_spec), **acc_spec},
             "train": {"pairs_rendered": args.train_pairs, "pairs_kept": n_train, "epochs": args.epochs,
                       "generation_s": gen_s, "train_s": train_s, "last_epoch_loss": hist[-1]},
             "launch": {"threads": threads, "pixels_per_thread": ppt},
-            "e2e": {"value": K * nb / (ms_e2e * 1e-3), "unit": "frames/s", "h2d_bytes_per_step": int(batch_bytes),
-                    "median_step_frames_per_s": nb / (float(np.median([s[0] for s in step_host])) * 1e-3),
+            "e2e": {"value": world * K * nb / (ms_e2e * 1e-3), "unit": "frames/s", "h2d_bytes_per_step": int(batch_bytes),
+                    "median_step_frames_per_s": world * nb / (float(np.median([s[0] for s in step_host])) * 1e-3),
                     "d2h_bytes_per_step": int(nb * ctypes_sizeof_result()), "h2d_gbs_alone": h2d_gbs,
                     "note": "copies of step k+1 (4 copy streams) overlap the tracking of step k (two input buffers)",
                     "steps_host_ms_track_host_ms_fallbacks_track_device_ms": step_host,
@@ -814,7 +814,7 @@ def measure_warm_batched(args, stream, local, world):
                                         "is not algorithmic traffic; it is inside `traffic`",
                          "kernel_ms": k_ms, "photometric_kernel_ms": s_ms, "iteration_ms": it_ms,
                          "iteration_frac": alg / (it_ms * 1e-3) / 1e9 / peak},
-            "plain_batched": {"frames_per_s": K * nb / (ms_p * 1e-3), "ms_per_step": ms_p / K,
+            "plain_batched": {"frames_per_s": world * K * nb / (ms_p * 1e-3), "ms_per_step": ms_p / K,
                               "schedule": "SO3 + 10/5/4, the reference's"},
             "accuracy": {"held_out_pairs": nbatch * nb, "warm_tuned": acc_tuned, "plain_batched": acc_plain,
                          "iterations_saved_tuned": saved(acc_tuned),
@@ -871,7 +871,7 @@ def measure_batched_verification(args, stream, world):
         ms = float(tt.item())
     done = np.array([r.done_us for r in res])
     err = np.array([synth.pose_error(result_pose(r), T) for r, T in zip(res, T2)])
-    return {"metric": "batched verification pairs/s", "value": n / (ms * 1e-3), "unit": "pairs/s",
+    return {"metric": "batched verification pairs/s", "value": world * n / (ms * 1e-3), "unit": "pairs/s",
             "steps": K, "ms_per_step": ms,
             "workload": f"{n} pairs per launch, sizes uniform over 160x120/320x240/640x480 "
                         f"({', '.join('%dx%d: %d' % (sizes[k] + (int((size_of == k).sum()),)) for k in range(3))}), "
