@@ -1271,7 +1271,7 @@ def run_warm_study(args):
     d = _errs(Pw, Pp)
     fail = lambda e: float(np.mean((e[:, 0] > np.radians(2.0)) | (e[:, 1] > 0.05)))
     pct = lambda v: {"p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90))}
-    judge = (ew > 1.5 * ep) | (d[:, 0] > np.radians(0.5))
+    disagree = (ew > 1.5 * ep) | (d[:, 0] > np.radians(0.5))
     # FP64 oracle on the first pairs (plain tracking of the same frames)
     from oracle import oracle
     orc = []
@@ -1305,7 +1305,7 @@ def run_warm_study(args):
                                 "warm": {"rot_rad": pct(err_w[:, 0]), "trans_m": pct(err_w[:, 1]), "fail": fail(err_w)}},
            "warm_vs_plain": {"within_1e-5": float(np.mean((d[:, 0] <= 1e-5) & (d[:, 1] <= 1e-5))),
                              "within_1e-4": float(np.mean((d[:, 0] <= 1e-4) & (d[:, 1] <= 1e-4))),
-                             "judged_disagreement_rate": float(np.mean(judge))},
+                             "disagreement_rate": float(np.mean(disagree))},
            "runtime_fallback_rate": float(np.mean(fb)),
            "iterations_mean": {"plain": itp.mean(axis=0).tolist(), "warm": itw.mean(axis=0).tolist()},
            "proposal_error_vs_gt": {"trans_m": pct(prop_err[0]), "rot_rad": pct(prop_err[1])},
