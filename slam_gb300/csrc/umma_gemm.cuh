@@ -194,16 +194,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
 // of B are 128 bytes apart along N and BN * 16 bytes apart along K; the
 // stage's "full" mbarrier counts the bytes in and the MMA issuer waits on
 // it.  A (the implicit im2col rows) stays on cp.async.
-//
-// Persistent over output tiles: CTA x of a grid of gridDim.x CTAs computes
-// the 128-row tiles x, x + gridDim.x, ... of its BN columns, and the K
-// chunks of consecutive tiles form one stream through the stages, so the
-// first chunks of the next tile are already loading while the epilogue of
-// the current one reads the accumulator.  TMEM and the barriers are set up
-// once per CTA.
 template <int BN, bool F16, int S, bool TMAB, class LA, class LB, class EP>
 __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, EP ep, int M, int N, int kchunks,
-                                                                  int *err, const __grid_constant__ CUtensorMap tmb) {
+                                                                  int chunks_per_split, int *err,
+                                                                  const __grid_constant__ CUtensorMap tmb) {
     static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "BN");
     static_assert(S >= 2 && S <= 6, "stages");
     constexpr int A_BYTES = 128 * kGemmKChunk * 2, B_BYTES = BN * kGemmKChunk * 2, STAGE = A_BYTES + B_BYTES;
@@ -216,12 +210,11 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
     __shared__ uint32_t tmem_base;
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n0 = blockIdx.y * BN;
-    const int nch = kchunks;
-    const int ntm = (M + 127) / 128;
-    if (nch <= 0 || (int)blockIdx.x >= ntm) return;
-    const int ntiles = (ntm - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int G = ntiles * nch;  // K chunks this CTA streams
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+    const int c_begin = blockIdx.z * chunks_per_split;
+    const int c_end = min(kchunks, c_begin + chunks_per_split);
+    const int nch = c_end - c_begin;
+    if (nch <= 0) return;
     if (warp == 0) {
         umma::tmem_alloc(&tmem_base, BN < 32 ? 32 : BN);
         umma::tmem_relinquish();
@@ -241,37 +234,30 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
     // slots as in k_umma_gemm: thread t fills the 16-byte slots t + 128 j
     constexpr int AR = 8, BR = BN / 16;
     const int kg = (tid >> 3) & 7;
-    auto tile_m0 = [&](int ti) { return ((int)blockIdx.x + ti * (int)gridDim.x) * 128; };
     typename LA::Row ra[AR];
-    int ra_tile = -1;  // tile whose row handles ra holds (loads are issued in tile order)
+#pragma unroll
+    for (int j = 0; j < AR; ++j) ra[j] = la.row(m0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
     typename LB::Row rb[TMAB ? 1 : BR];
     if constexpr (!TMAB) {
 #pragma unroll
         for (int j = 0; j < BR; ++j) rb[j] = lb.row(n0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
     }
-    auto issue = [&](int g) {
-        const int ti = g / nch, c = g - ti * nch;
-        if (ti != ra_tile) {
-            const int m0 = tile_m0(ti);
-#pragma unroll
-            for (int j = 0; j < AR; ++j) ra[j] = la.row(m0 + (((tid >> 6) + 2 * j) << 3) + (tid & 7));
-            ra_tile = ti;
-        }
-        uint8_t *sa = smem + (g % S) * STAGE;
+    auto issue = [&](int c) {
+        uint8_t *sa = smem + (c % S) * STAGE;
         uint8_t *sb = sa + A_BYTES;
-        const int k8 = c * (kGemmKChunk / 8) + kg;
+        const int k8 = (c_begin + c) * (kGemmKChunk / 8) + kg;
         const typename LA::Col ca = la.col(k8);
 #pragma unroll
         for (int j = 0; j < AR; ++j) {
             int bytes;
-            const void *gp = la.src(ra[j], ca, bytes);
-            cp_async16(sa + (tid + 128 * j) * 16, gp, bytes);
+            const void *g = la.src(ra[j], ca, bytes);
+            cp_async16(sa + (tid + 128 * j) * 16, g, bytes);
         }
         if constexpr (TMAB) {
             if (tid == 0) {
-                uint64_t *bar = &full[g % S];
+                uint64_t *bar = &full[c % S];
                 mbar_expect_tx(bar, (uint32_t)B_BYTES);
-                const int kx = c * kGemmKChunk;
+                const int kx = (c_begin + c) * kGemmKChunk;
 #pragma unroll
                 for (int j = 0; j < kGemmKChunk / 8; ++j) tma_load_2d(sb + j * BN * 16, &tmb, kx + 8 * j, n0, bar);
             }
@@ -280,41 +266,39 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
 #pragma unroll
             for (int j = 0; j < BR; ++j) {
                 int bytes;
-                const void *gp = lb.src(rb[j], cb, bytes);
-                cp_async16(sb + (tid + 128 * j) * 16, gp, bytes);
+                const void *g = lb.src(rb[j], cb, bytes);
+                cp_async16(sb + (tid + 128 * j) * 16, g, bytes);
             }
         }
     };
     int issued = 0;  // chunks whose loads were issued
 #pragma unroll
     for (int p = 0; p < S - 1; ++p) {
-        if (p < G) {
+        if (p < nch) {
             issue(p);
             issued = p + 1;
         }
         cp_async_group();
     }
     bool ok = true;
-    int g = 0;
-    int mma_done = 0;  // chunks whose MMAs are known complete
-    for (; g < G; ++g) {
-        const int s = g % S, ti = g / nch, c = g - ti * nch;
-        // refill the stage the MMAs of chunk g - 1 read, with chunk g + S - 1
-        const int pf = g + S - 1;
-        if (pf < G) {
-            if (g >= 1 && mma_done < g) {
-                ok = umma::mbar_wait(&mbar[(g - 1) % S], ((g - 1) / S) & 1, kGemmWaitPolls);
+    int c = 0;
+    for (; c < nch; ++c) {
+        const int s = c % S;
+        // refill the stage the MMAs of chunk c - 1 read, with chunk c + S - 1
+        const int pf = c + S - 1;
+        if (pf < nch) {
+            if (c >= 1) {
+                ok = umma::mbar_wait(&mbar[(c - 1) % S], ((c - 1) / S) & 1, kGemmWaitPolls);
                 if (!__syncthreads_and(ok)) break;
-                mma_done = g;
             }
             issue(pf);
             issued = pf + 1;
         }
         cp_async_group();
-        cp_async_wait_groups<S - 1>();  // this thread's copies of chunk g have landed
+        cp_async_wait_groups<S - 1>();  // this thread's copies of chunk c have landed
         umma::fence_smem_to_async();
         bool bok = true;
-        if (TMAB && tid == 0) bok = umma::mbar_wait(&full[s], (g / S) & 1, kGemmWaitPolls);
+        if (TMAB && tid == 0) bok = umma::mbar_wait(&full[s], (c / S) & 1, kGemmWaitPolls);
         if (!__syncthreads_and(bok)) {
             ok = false;
             break;
@@ -328,38 +312,31 @@ __global__ void __launch_bounds__(kGemmThreads) k_umma_gemm_async(LA la, LB lb, 
                                umma::smem_desc(b0 + k * 2 * B_LBO, B_LBO, B_SBO), IDESC, (c > 0 || k > 0) ? 1u : 0u);
             umma::mma_commit(&mbar[s]);
         }
-        if (c == nch - 1) {
-            // the tile's last chunk: its MMAs done, read the accumulator out
-            ok = umma::mbar_wait(&mbar[s], (g / S) & 1, kGemmWaitPolls);
-            if (!__syncthreads_and(ok)) {
-                ++g;
-                break;
-            }
-            mma_done = g + 1;
-            umma::fence_after_sync();
-            const int row = tile_m0(ti) + warp * 32 + lane;
-            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-            for (int j = 0; j < BN; j += 8) {
-                float v[8];
-                umma::tmem_ld8(trow + j, v);
-                if (row < M && n0 + j < N) ep(row, n0 + j, v);
-            }
-            // every warp's accumulator reads are done before the next tile's MMAs
-            umma::fence_before_sync();
-            __syncthreads();
-        }
     }
     cp_async_wait_groups<0>();
     // TMA boxes still in flight (a loop left early): wait for them (bounded)
     // before the CTA's shared memory can go away
     if (TMAB && tid == 0)
-        for (int q = g; q < issued; ++q) umma::mbar_wait(&full[q % S], (q / S) & 1, kGemmWaitPolls);
-    // MMAs still running (a loop left early): the last commit covers them
+        for (int q = c; q < issued; ++q) umma::mbar_wait(&full[q % S], (q / S) & 1, kGemmWaitPolls);
     bool drained = true;
-    if (g > mma_done && g > 0) drained = umma::mbar_wait(&mbar[(g - 1) % S], ((g - 1) / S) & 1, kGemmWaitPolls);
-    ok = __syncthreads_and(ok && drained) && g == G;
-    if (!ok && tid == 0 && err) atomicExch(err, 1);
+    if (c > 0) {
+        const int last = c - 1;
+        drained = umma::mbar_wait(&mbar[last % S], (last / S) & 1, kGemmWaitPolls);
+    }
+    ok = __syncthreads_and(ok && drained) && c == nch;
+    umma::fence_after_sync();
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int j = 0; j < BN; j += 8) {
+            float v[8];
+            umma::tmem_ld8(trow + j, v);
+            if (row < M && n0 + j < N) ep(row, n0 + j, v);
+        }
+    } else if (tid == 0 && err) {
+        atomicExch(err, 1);
+    }
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, BN < 32 ? 32 : BN);
@@ -378,34 +355,28 @@ cudaError_t launch_umma_gemm_async(const LA &la, const LB &lb, const EP &ep, int
     if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
     const int kchunks = (K + kGemmKChunk - 1) / kGemmKChunk;
     constexpr int smem = gemm_async_smem_bytes<BN, S>();
-    // persistent grid: as many CTAs per column block as fit on the GPU at
-    // once (never more than the 128-row tiles)
-    static int resident[2] = {0, 0};  // per instantiation: CTAs per SM without / with TMA
-    static int sms = 0;
-    const int ntm = (M + 127) / 128, nbn = (N + BN - 1) / BN;
-    auto kern_t = k_umma_gemm_async<BN, F16, S, true, LA, LB, EP>;
-    auto kern_c = k_umma_gemm_async<BN, F16, S, false, LA, LB, EP>;
-    const int w = tmb ? 1 : 0;
-    if (!resident[w]) {
-        cudaError_t e = cudaFuncSetAttribute(tmb ? kern_t : kern_c, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        int dev = 0, r = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, tmb ? kern_t : kern_c, kGemmThreads, smem)) !=
-            cudaSuccess)
-            return e;
-        resident[w] = r > 0 ? r : 1;
-    }
-    int gx = (sms * resident[w] + nbn - 1) / nbn;
-    if (gx > ntm) gx = ntm;
-    if (gx < 1) gx = 1;
-    dim3 grid(gx, nbn, 1);
+    dim3 grid((M + 127) / 128, (N + BN - 1) / BN, 1);
     if (tmb) {
-        kern_t<<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, err, *tmb);
+        static bool attr_set = false;  // per instantiation
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_async<BN, F16, S, true, LA, LB, EP>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+        k_umma_gemm_async<BN, F16, S, true, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks,
+                                                                                        kchunks, err, *tmb);
     } else {
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_async<BN, F16, S, false, LA, LB, EP>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
         CUtensorMap none{};
-        kern_c<<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks, err, none);
+        k_umma_gemm_async<BN, F16, S, false, LA, LB, EP><<<grid, kGemmThreads, smem, s>>>(la, lb, ep, M, N, kchunks,
+                                                                                         kchunks, err, none);
     }
     return cudaGetLastError();
 }
