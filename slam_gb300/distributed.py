@@ -6,9 +6,6 @@ verification workload) shard by pair index with no data-path collective.
 These helpers cover the host side: the contiguous share of pairs of a rank,
 the gather of per-pair results on the host, and the whole-job timing (the
 slowest rank's time, every rank's work)."""
-import numpy as np
-
-
 def shard(n, rank, world):
     """[begin, end) of the pairs rank `rank` of `world` tracks: contiguous
     shares whose sizes differ by at most one."""
@@ -57,7 +54,3 @@ def job_rate(units_per_rank, seconds_per_rank):
     world = 1 if dist is None else dist.get_world_size()
     return world * units_per_rank / max_over_ranks(seconds_per_rank)
 
-
-def result_poses(results):
-    """[n, 4, 4] poses of gathered odo_pair_result records."""
-    return np.array([np.array(r.pose, np.float64).reshape(4, 4) if hasattr(r, "pose") else r for r in results])
