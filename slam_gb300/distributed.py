@@ -6,6 +6,8 @@ verification workload) shard by pair index with no data-path collective.
 These helpers cover the host side: the contiguous share of pairs of a rank,
 the gather of per-pair results on the host, and the whole-job timing (the
 slowest rank's time, every rank's work)."""
+
+
 def shard(n, rank, world):
     """[begin, end) of the pairs rank `rank` of `world` tracks: contiguous
     shares whose sizes differ by at most one."""
