@@ -271,6 +271,18 @@ class OracleRuns:
     def _fp32_runs(self):
         return [("main", self.run(32))] + [(k, self.run(*PERTURBATIONS[k])) for k in self._perturbed() if k != "fp64"]
 
+    def matches_a_tie_run(self, tg, Rg):
+        """True when the GPU pose is within the flat 1e-5 of one of the oracle
+        runs whose flagged rounding ties were decided the other way (the GPU
+        took a set of tie decisions the oracle's IEEE arithmetic takes
+        differently)."""
+        for k in TIE_RUNS:
+            t, R, _ = self.run(*PERTURBATIONS[k])
+            rot, tr = pose_diff(tg, Rg, t, R)
+            if rot <= POSE_TOL_RAD and tr <= POSE_TOL_M:
+                return True
+        return False
+
     def closest_run(self, tg, Rg):
         """(name, (rad, m)) of the FP32 run (unperturbed or perturbed) closest
         to a GPU pose."""

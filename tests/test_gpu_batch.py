@@ -42,7 +42,7 @@ def to_batch(pairs):
 
 def check_against_oracle(pairs, res, flags, tag):
     from slam_gb300.batch import result_pose
-    flat = undetermined = determined_wide = 0
+    flat = undetermined = determined_wide = tie_explained = 0
     worst = (0.0, 0.0)
     for i, p in enumerate(pairs):
         ref = frame_runs(p, flags, levels=p["levels"], images=pair_images(p))
@@ -54,8 +54,9 @@ def check_against_oracle(pairs, res, flags, tag):
             undetermined += 1
             continue
         flat += is_flat
-        if not is_flat:
-            determined_wide += ref.summation_gap() < GAP_LIMIT
+        if not is_flat and ref.summation_gap() < GAP_LIMIT:
+            determined_wide += 1
+            tie_explained += ref.matches_a_tie_run(T[:3, 3], T[:3, :3])
         worst = (max(worst[0], rot), max(worst[1], tr))
         assert ref.iterations_ok(res[i].iterations), (label, list(res[i].iterations), o.iterations())
         st = o.stats
@@ -63,8 +64,9 @@ def check_against_oracle(pairs, res, flags, tag):
             assert ref.count_ok(name, getattr(res[i], name), is_flat), (label, name, getattr(res[i], name), st[name])
     report("%s: %d/%d pairs within the flat 1e-5 bound, %d undetermined by the reference algorithm, max pose "
            "diff of the others %.2e rad %.2e m; of the pairs beyond 1e-5, %d have an oracle pose that moves by less "
-           "than %.0e under another summation order and in FP64" % (tag, flat, len(pairs), undetermined, worst[0],
-                                                                    worst[1], determined_wide, GAP_LIMIT))
+           "than %.0e under another summation order and in FP64, and %d of those are within 1e-5 of an oracle run "
+           "with some rounding ties decided the other way" % (tag, flat, len(pairs), undetermined, worst[0], worst[1],
+                                                              determined_wide, GAP_LIMIT, tie_explained))
 
 
 FLAGS = [dict(), dict(so3=False), dict(icpWeight=100.0, so3=False), dict(rgbOnly=True, so3=False)]

@@ -35,7 +35,7 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
     prev = synth.render(scene, T[0], cam, noise_seed=seed * 100003, depth=False, rgba=True)
     g.initFirstRGB(dev(prev["rgba"]))
     est = [T[0].astype(np.float32).astype(np.float64)]
-    rot_err, tr_err, jtj_err, flat_frames, determined = [], [], [], [], []
+    rot_err, tr_err, jtj_err, flat_frames, determined, tie_explained = [], [], [], [], [], []
     for k in range(1, FRAMES):
         start = est[-1].astype(np.float32)
         model = synth.render(scene, start.astype(np.float64), cam, depth=False, rgba=True, model=True)
@@ -75,6 +75,7 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
         jtj_err.append(jtj)
         flat_frames.append(flat)
         determined.append(ref.summation_gap() < GAP_LIMIT)
+        tie_explained.append(determined[-1] and not flat and ref.matches_a_tie_run(tg, Rg))
         est.append(synth.pose(Ro, to))
         prev = live
     rot_err, tr_err, jtj_err, flat_frames, determined = (np.array(v) for v in (rot_err, tr_err, jtj_err, flat_frames,
@@ -91,4 +92,6 @@ def test_trajectory_frame_to_model_matches_oracle(gpu):
               rpe["trans_rmse"], np.degrees(rpe["rot_rmse"])))
     report("trajectory: on %d of %d frames the oracle's own pose moves by less than %.0e under another summation "
            "order and in FP64 (the reference algorithm determines the pose there); the GPU is within the flat 1e-5 "
-           "on %d of them" % (determined.sum(), len(determined), GAP_LIMIT, (determined & flat_frames).sum()))
+           "on %d of them and within 1e-5 of an oracle run with some rounding ties decided the other way on %d of the "
+           "others" % (determined.sum(), len(determined), GAP_LIMIT, (determined & flat_frames).sum(),
+                       sum(tie_explained)))
