@@ -379,7 +379,12 @@ def run_ours(args):
     alg_bytes = BYTES_PER_PX_ITER * n0
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-    launches_per_frame = 10 + 4 + 2 * (10 + 5 + 4)
+    # per frame: the init calls (model maps; model depth + intensity and two
+    # pyramid steps; two depth pyramid steps and the maps; live depth +
+    # intensity and two pyramid steps = 10), then the tracking call (state
+    # copy in, derivatives, SO3, begin, end, state copy out = 6) and two
+    # kernels per iteration of 10/5/4
+    launches_per_frame = 10 + 6 + 2 * (10 + 5 + 4)
 
     out = None
     if rank == 0:
@@ -773,15 +778,19 @@ def measure_warm_batched(args, stream, local, world):
     peak, peak_kind = measured_peaks()
     achieved = alg / (k_ms * 1e-3) / 1e9
     traffic_px = profile_traffic(TRAFFIC_PROFILE_BATCH)
-    # kernels per warm step: packing + 8 GEMMs per 256 pairs, the warm graph
-    # (stamp, model maps, 2 photometric inputs, 4 pyramid steps, 2 depth
-    # pyramid steps, maps, derivatives, begin, seed, 3 per iteration, end) and
-    # the fall-back batch with its SO3 stage
+    # kernels per warm step: the network (per 256 pairs: argument copy,
+    # packing, 8 GEMMs; then the time-out flag copy), the warm graph
+    # (argument and state copies in, stamp, model maps, 2 photometric inputs,
+    # 4 pyramid steps, 2 depth pyramid steps, maps, derivatives, begin, seed,
+    # 3 per iteration, end, state copy out), the proposals' copy out, and the
+    # fall-back batch (copies in, stamp, its photometric input and 2 pyramid
+    # steps for the SO3 stage, SO3, begin, 3 per iteration of 10/5/4, end,
+    # copy out)
     fbr = acc_tuned["fallback_rate"]
-    gemm = -(-nb // 256) * 9
-    warm_graph = 13 + 3 * sum(its[:args.warm_levels])
-    plain_graph = 14 + 1 + 3 * 19
-    launches = K * (gemm + warm_graph + (plain_graph if fbr > 0 else 0))
+    net_k = -(-nb // 256) * 10 + 1
+    warm_graph = 18 + 3 * sum(its[:args.warm_levels])
+    fallback = 10 + 3 * 19
+    launches = K * (net_k + warm_graph + 1 + (fallback if fbr > 0 else 0))
     return {"fps": world * K * nb / (ms_w * 1e-3), "ms_per_step": ms_w / K, "steps": K, "warmup": W, "batch_pairs": nb,
             "eval_pairs": nbatch * nb, "pool_batches": nbatch, "batch_bytes": batch_bytes,
             "schedule": {"levels": args.warm_levels, "iterations": list(its), "so3": False},
