@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--save-params", default=None)
     ap.add_argument("--load-params", default=None, help="warm study: skip training, use these parameters")
     ap.add_argument("--sweep", action="store_true", help="warm study: also evaluate other warm schedules")
-    ap.add_argument("--batch-pairs", type=int, default=500, help="pairs per warm-started batched step")
+    ap.add_argument("--batch-pairs", type=int, default=1000, help="pairs per warm-started batched step")
     ap.add_argument("--verify-pairs", type=int, default=512,
                     help="pairs per launch of the batched-verification line (0: skip it)")
     ap.add_argument("--residual-ratio", type=float, default=6.0)
