@@ -617,7 +617,8 @@ def measure_warm_batched(args, stream, local, world):
     cam = synth.Camera()
     nb = args.batch_pairs
     b = BatchOdometry(nb, stream=stream.cuda_stream)
-    net = ws.WarmStartNet(max_batch=256, stream=stream.cuda_stream)
+    # the whole step's proposals in one forward pass (training uses 256)
+    net = ws.WarmStartNet(max_batch=max(256, nb), stream=stream.cuda_stream)
     t0 = time.time()
     ts = ws.make_training_set(net, b, args.seed * 17 + 3, args.train_pairs)
     net.set_loss_metric(ts["metric"])
@@ -787,7 +788,7 @@ def measure_warm_batched(args, stream, local, world):
     # steps for the SO3 stage, SO3, begin, 3 per iteration of 10/5/4, end,
     # copy out)
     fbr = acc_tuned["fallback_rate"]
-    net_k = -(-nb // 256) * 10 + 1
+    net_k = -(-nb // max(256, nb)) * 10 + 1
     warm_graph = 18 + 3 * sum(its[:args.warm_levels])
     fallback = 10 + 3 * 19
     launches = K * (net_k + warm_graph + 1 + (fallback if fbr > 0 else 0))
