@@ -1212,9 +1212,8 @@ def run_warm_study(args):
             if args.sweep:
                 rp0 = b.track(fps, descs=descs)
                 Pp0 = _res_array(rp0)[0]
-                for lv, it_ in ((3, (1, 2, 2)), (3, (2, 1, 1)), (3, (2, 2, 1)), (3, (2, 2, 2)), (3, (3, 2, 2)),
-                                (2, (2, 2, 0))):
-                    for ratio in (4.0, 6.0, 8.0):
+                for lv, it_ in ((3, (1, 2, 2)), (3, (2, 2, 1)), (3, (2, 2, 2)), (3, (3, 2, 2))):
+                    for ratio in (6.0, 8.0, 12.0, 16.0):
                         kw = dict(wkw, levels=lv, iterations=it_, residual_limit=ratio * plain_res)
                         b.track_warm(net, fps, descs=descs, **kw)
                         torch.cuda.synchronize()
@@ -1227,6 +1226,8 @@ def run_warm_study(args):
                         sweep.append({"levels": lv, "iterations": list(it_), "residual_ratio": ratio,
                                       "fps": m / tt, "fallback": float(fb0.mean()),
                                       "rot_p50": float(np.median(ee[:, 0])), "trans_p50": float(np.median(ee[:, 1])),
+                                      "rot_p90": float(np.percentile(ee[:, 0], 90)),
+                                      "trans_p90": float(np.percentile(ee[:, 1], 90)),
                                       "fail": float(np.mean((ee[:, 0] > np.radians(2)) | (ee[:, 1] > 0.05)))})
         rp = b.track(fps, descs=descs)                      # warm-up (graph instantiation)
         rw, fb = b.track_warm(net, fps, descs=descs, **wkw)
