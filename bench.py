@@ -93,7 +93,7 @@ def parse():
     ap.add_argument("--batch-pairs", type=int, default=1000, help="pairs per warm-started batched step")
     ap.add_argument("--verify-pairs", type=int, default=512,
                     help="pairs per launch of the batched-verification line (0: skip it)")
-    ap.add_argument("--residual-ratio", type=float, default=6.0)
+    ap.add_argument("--residual-ratio", type=float, default=16.0)
     ap.add_argument("--front-end", type=int, default=1,
                     help="also time the producers of the tracker's inputs (depth pre-filter, model prediction, "
                          "fill-in) at 640x480")
