@@ -22,6 +22,9 @@ constexpr int BX = 32, BY = 8;
 // batches (a block's memory round trip shared by 1024 outputs), 8 for a
 // single frame (enough blocks to fill the GPU from one 640x480 image).
 constexpr int kTileRowsBatch = 32, kTileRowsSingle = 8;
+// The Gaussian pyramid's batched tiles are 16 rows high: its staged tiles
+// and horizontal sums for 32 rows would exceed 48 KB of static shared memory.
+constexpr int kGaussRowsBatch = 16;
 
 // Linear enumeration of the 32 x th tiles of all pyramid levels (level l is
 // (cols >> l) x (rows >> l)), so that a multi-level launch has no blocks for
@@ -46,23 +49,27 @@ inline LevelTiles level_tiles(int cols, int rows, int nlevels, int th) {
     return t;
 }
 // Level and first pixel (X0, Y0) of linear tile b.
+// (Selects, not an indexed read: a dynamically indexed kernel-parameter
+// array is copied to local memory.)
 __device__ __forceinline__ void tile_origin(const LevelTiles &t, int b, int &l, int &X0, int &Y0) {
     l = b >= t.start[2] ? 2 : (b >= t.start[1] ? 1 : 0);
-    const int k = b - t.start[l];
-    X0 = (k % t.tx[l]) * BX;
-    Y0 = (k / t.tx[l]) * t.th;
+    const int k = b - (l == 2 ? t.start[2] : (l == 1 ? t.start[1] : t.start[0]));
+    const int tx = l == 2 ? t.tx[2] : (l == 1 ? t.tx[1] : t.tx[0]);
+    X0 = (k % tx) * BX;
+    Y0 = (k / tx) * t.th;
 }
 
 // The window kernels stage the source pixels of their block in shared
-// memory (coalesced loads, each source pixel read once) and then run the
-// reference's window loops unchanged on the tile.  A block of 32x8 threads
-// computes 32 x TR outputs (TR / 8 per thread, rows 8 apart).  A 2x
-// downsampling 5x5 window of those outputs covers source columns
-// [2 X0 - 2, 2 X0 + 65) and rows [2 Y0 - 2, 2 Y0 + 2 TR + 1); the same-level
-// 3x3 / 4x4 windows of the derivative kernel cover [X0 - 2, X0 + 33) x
-// [Y0 - 2, Y0 + TR + 1).  Tile entries outside the image are never read
-// (the loops clamp to the image).
-constexpr int kDownTW = 2 * BX + 4, kDerTW = BX + 4;
+// memory (coalesced loads, each source pixel read once) and then evaluate
+// the reference's windows on the tile.  A block of 32x8 threads computes
+// 32 x TR outputs (TR / 8 per thread, rows 8 apart).  A 2x downsampling 5x5
+// window of those outputs covers source columns [2 X0 - 2, 2 X0 + 65) and
+// rows [2 Y0 - 2, 2 Y0 + 2 TR + 1); the same-level 3x3 / 4x4 windows of the
+// derivative kernel cover [X0 - 2, X0 + 33) x [Y0 - 2, Y0 + TR + 1).  The
+// Gaussian and derivative tiles start at a multiple of 4 columns and are a
+// few columns wider, so 4-pixel loads fill them.  Tile entries outside the
+// image are never read by the border loops (they clamp to the image).
+constexpr int kDownTW = 2 * BX + 4;
 
 // The batched kernels read their pair's argument block from a device array.
 // Read there directly, every field would be re-loaded from global memory
@@ -87,8 +94,8 @@ __host__ __device__ constexpr int der_th() { return TR + 4; }
 // All loads of a thread are issued before the first store to shared memory
 // (a register array of compile-time size), so a block waits for one memory
 // round trip, not one per element.  Blocks are BX x BY threads.
-template <typename T, int TH, int TW>
-__device__ __forceinline__ void load_tile(const Img<const T> &src, int ox, int oy, T (&tile)[TH][TW]) {
+template <typename T, typename S, int TH, int TW>
+__device__ __forceinline__ void load_tile(const Img<const T> &src, int ox, int oy, S (&tile)[TH][TW]) {
     constexpr int N = TH * TW, NT = BX * BY, IT = (N + NT - 1) / NT;
     const int tid = threadIdx.y * BX + threadIdx.x;
     T v[IT];
@@ -100,10 +107,10 @@ __device__ __forceinline__ void load_tile(const Img<const T> &src, int ox, int o
         v[k] = T{};
         if (i < N && gx >= 0 && gy >= 0 && gx < src.cols && gy < src.rows) v[k] = at(src, gx, gy);
     }
-    T *flat = &tile[0][0];
+    S *flat = &tile[0][0];
 #pragma unroll
     for (int k = 0; k < IT; ++k)
-        if (tid + k * NT < N) flat[tid + k * NT] = v[k];
+        if (tid + k * NT < N) flat[tid + k * NT] = (S)v[k];
 }
 
 // pyrDownGaussKernel, src/odom/utils.cu:57-94 (sigma_color = 30, :103), on
@@ -393,9 +400,115 @@ __host__ __device__ constexpr int gauss_w(int i, int j) {
 // pyrDownKernelIntensityGauss (src/odom/utils.cu:470-500) in one launch:
 // masked 5x5 Gaussian, window clamped at cols-1/rows-1 (exclusive), reversed
 // kernel index, int count.
+//
+// The block's source pixels are staged once per tile as
+//   d[r][c]  the depth, a NaN stored as +0, and
+//   w[r][c]  intensity | (intensity > 0) << 12 | (depth not NaN) << 20.
+// Interior outputs (the full 5x5 window inside the image, where the
+// reversed index equals the forward one: the weights are symmetric):
+//  * intensity sum and both counts are integers (weights 1 4 6 4 1 per
+//    axis, products <= 36), and every partial sum of the reference's float
+//    intensity loop is an integer below 2^24, hence exact; so they are sums
+//    in any order, and separable: a horizontal pass computes, for every
+//    staged row and output column, the three 5-tap sums at once on the
+//    packed word (fields <= 16 * 255 < 2^12, <= 16 < 2^8, <= 16 < 2^12), and
+//    each output adds five of them with the vertical weights (intensity sum
+//    <= 65280 and the counts <= 256 each in 16-bit fields);
+//  * the depth sum is the reference's chain of 25 fused multiply-adds in its
+//    order, over the zeroed tile: a NaN tap contributes fma(+0, w, s) = s
+//    (s is never -0: it starts at +0 and no round-to-nearest sum of these
+//    terms is -0), the same value as skipping it.
+// Border outputs run the reference's loops on the same tiles.
+// The staged tile starts 4 source columns left of the block's first
+// window column pair (2 X0 - 4, a multiple of 4) and is 2 BX + 8 wide, so
+// that it is filled by aligned 4-pixel loads.
+constexpr int kGaussTW = 2 * BX + 8;
 template <int TR>
-__device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[down_th<TR>()][kDownTW],
-                                          const uint8_t (&it)[down_th<TR>()][kDownTW], int ox, int oy, int x, int y) {
+struct GaussTile {
+    static constexpr int TH = down_th<TR>();
+    __align__(16) float d[TH][kGaussTW];
+    __align__(16) unsigned w[TH][kGaussTW];
+    unsigned hs[TH][BX];  // horizontal weighted intensity sums
+    unsigned hc[TH][BX];  // horizontal weighted counts: intensity | depth << 16
+};
+constexpr unsigned kGaussNz = 1u << 12, kGaussValid = 1u << 20;
+
+// Stages source columns [ox, ox + kGaussTW) x rows [oy, oy + TH), ox a
+// multiple of 4: one 4-byte intensity load and one 16-byte depth load per
+// 4 pixels where the 4 pixels lie inside the image and the rows are
+// aligned, pixel by pixel at the image's edges.  All loads of a thread are
+// issued before its first shared-memory store.
+template <int TR>
+__device__ __forceinline__ void gauss_stage(const GaussArgs &a, int ox, int oy, GaussTile<TR> &g) {
+    constexpr int Q = kGaussTW / 4, N = GaussTile<TR>::TH * Q, NT = BX * BY, IT = (N + NT - 1) / NT;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    const Img<const uint8_t> isrc = a.isrc;
+    const Img<const float> dsrc = a.dsrc;
+    const bool dep = a.do_depth != 0;
+    const bool aligned = !(((uintptr_t)isrc.data | isrc.pitch) & 3) &&
+                         (!dep || !(((uintptr_t)dsrc.data | dsrc.pitch) & 15));
+    unsigned iv[IT];
+    float4 dv[IT];
+#pragma unroll
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
+        const int ty = i / Q, gx = ox + 4 * (i - ty * Q), gy = oy + ty;
+        const float q = qnan_f();
+        iv[k] = 0;
+        dv[k] = make_float4(q, q, q, q);
+        if (i < N && gy >= 0 && gy < isrc.rows) {
+            if (aligned && gx >= 0 && gx + 3 < isrc.cols) {
+                iv[k] = *reinterpret_cast<const unsigned *>(&at(isrc, gx, gy));
+                if (dep) dv[k] = *reinterpret_cast<const float4 *>(&at(dsrc, gx, gy));
+            } else {
+                float d4[4] = {q, q, q, q};
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (gx + e >= 0 && gx + e < isrc.cols) {
+                        iv[k] |= (unsigned)at(isrc, gx + e, gy) << (8 * e);
+                        if (dep) d4[e] = at(dsrc, gx + e, gy);
+                    }
+                dv[k] = make_float4(d4[0], d4[1], d4[2], d4[3]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
+        if (i < N) {
+            const int ty = i / Q, tx = 4 * (i - ty * Q);
+            const float d4[4] = {dv[k].x, dv[k].y, dv[k].z, dv[k].w};
+            float o[4];
+            unsigned w[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const unsigned v = (iv[k] >> (8 * e)) & 0xffu;
+                const bool ok = !isnan(d4[e]);
+                o[e] = ok ? d4[e] : 0.f;
+                w[e] = v | (v > 0 ? kGaussNz : 0u) | (ok ? kGaussValid : 0u);
+            }
+            *reinterpret_cast<float4 *>(&g.d[ty][tx]) = make_float4(o[0], o[1], o[2], o[3]);
+            *reinterpret_cast<uint4 *>(&g.w[ty][tx]) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
+// Horizontal 5-tap sums of every staged row at the 32 output columns
+// (output column X0 + j reads staged columns 2 j + 2 .. 2 j + 6).
+template <int TR>
+__device__ __forceinline__ void gauss_rows(GaussTile<TR> &g) {
+    const int tid = threadIdx.y * BX + threadIdx.x, lane = threadIdx.x;
+    for (int r = tid >> 5; r < GaussTile<TR>::TH; r += BY) {
+        const unsigned *p = &g.w[r][2 * lane + 2];
+        const uint2 w01 = *reinterpret_cast<const uint2 *>(p), w23 = *reinterpret_cast<const uint2 *>(p + 2);
+        const unsigned h = (w01.x + p[4]) + 4u * (w01.y + w23.y) + 6u * w23.x;
+        g.hs[r][lane] = h & 0xfffu;
+        g.hc[r][lane] = ((h >> 12) & 0xffu) | ((h >> 20) << 16);
+    }
+}
+
+template <int TR>
+__device__ __forceinline__ void gauss_out(const GaussArgs &a, const GaussTile<TR> &g, int ox, int oy, int x, int y) {
     const Img<float> ddst = a.ddst;
     const Img<const uint8_t> isrc = a.isrc;
     const Img<uint8_t> idst = a.idst;
@@ -405,34 +518,41 @@ __device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[
     int tx = min(2 * x - D / 2 + D, isrc.cols - 1);
     int ty = min(2 * y - D / 2 + D, isrc.rows - 1);
     const int cy0 = max(0, 2 * y - D / 2), cx0 = max(0, 2 * x - D / 2);
-    // interior: the same loops fully unrolled (ty - cy - 1 = 4 - i, tx - cx - 1 = 4 - j)
     const bool interior = cx0 == 2 * x - 2 && tx == 2 * x + 3 && cy0 == 2 * y - 2 && ty == 2 * y + 3;
+    if (interior) {
+        const int r0 = cy0 - oy, c0 = cx0 - ox;  // even: 2 (y - Y0), 2 (x - X0) + 2
+        constexpr unsigned wv[5] = {1, 4, 6, 4, 1};
+        unsigned isum = 0, cnt = 0;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            isum += wv[i] * g.hs[r0 + i][(c0 - 2) >> 1];
+            cnt += wv[i] * g.hc[r0 + i][(c0 - 2) >> 1];
+        }
+        if (do_depth) {
+            float sum = 0;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                const float *r = &g.d[r0 + i][c0];
+                const float2 d01 = *reinterpret_cast<const float2 *>(r), d23 = *reinterpret_cast<const float2 *>(r + 2);
+                const float v[5] = {d01.x, d01.y, d23.x, d23.y, r[4]};
+#pragma unroll
+                for (int j = 0; j < 5; ++j) sum = __fmaf_rn(v[j], (float)gauss_w(4 - i, 4 - j), sum);
+            }
+            at(ddst, x, y) = (float)(sum / (float)(int)(cnt >> 16));
+        }
+        at(idst, x, y) = ((float)isum / (float)(int)(cnt & 0xffffu));
+        return;
+    }
     if (do_depth) {
         float sum = 0;
         int count = 0;
-        if (interior) {
-#pragma unroll
-            for (int i = 0; i < 5; ++i) {
-                const float *r = dt[cy0 + i - oy] - ox + cx0;
-#pragma unroll
-                for (int j = 0; j < 5; ++j) {
-                    // branch-free: a masked tap adds +0 (sum >= 0: depths); the
-                    // fused multiply-add is the contraction the compiler makes
-                    // of the reference's `sum += r * w`
-                    const float v = r[j];
-                    const bool ok = !isnan(v);
-                    sum = __fmaf_rn(ok ? v : 0.f, (float)gauss_w(4 - i, 4 - j), sum);
-                    count += ok ? gauss_w(4 - i, 4 - j) : 0;
-                }
-            }
-        } else {
-            for (int cy = cy0; cy < ty; ++cy) {
-                const float *r = dt[cy - oy] - ox;
-                for (int cx = cx0; cx < tx; ++cx) {
-                    if (!isnan(r[cx])) {
-                        sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
-                        count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
-                    }
+        for (int cy = cy0; cy < ty; ++cy) {
+            const float *r = g.d[cy - oy] - ox;
+            const unsigned *m = g.w[cy - oy] - ox;
+            for (int cx = cx0; cx < tx; ++cx) {
+                if (m[cx] & kGaussValid) {
+                    sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+                    count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
                 }
             }
         }
@@ -441,30 +561,13 @@ __device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[
     {
         float sum = 0;
         int count = 0;
-        if (interior) {
-            // integer arithmetic: every partial sum of the reference's float
-            // loop is an integer below 2^24 (255 x 256), hence exact, so the
-            // integer sum converted to float is the same value
-            int isum = 0;
-#pragma unroll
-            for (int i = 0; i < 5; ++i) {
-                const uint8_t *r = it[cy0 + i - oy] - ox + cx0;
-#pragma unroll
-                for (int j = 0; j < 5; ++j) {
-                    const int v = r[j];
-                    isum += v * gauss_w(4 - i, 4 - j);
-                    count += v > 0 ? gauss_w(4 - i, 4 - j) : 0;
-                }
-            }
-            sum = (float)isum;
-        } else {
-            for (int cy = cy0; cy < ty; ++cy) {
-                const uint8_t *r = it[cy - oy] - ox;
-                for (int cx = cx0; cx < tx; ++cx) {
-                    if (r[cx] > 0) {
-                        sum += r[cx] * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
-                        count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
-                    }
+        for (int cy = cy0; cy < ty; ++cy) {
+            const unsigned *r = g.w[cy - oy] - ox;
+            for (int cx = cx0; cx < tx; ++cx) {
+                const int v = r[cx] & 0xffu;
+                if (v > 0) {
+                    sum += v * c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
+                    count += c_gauss5x5[(ty - cy - 1) * 5 + (tx - cx - 1)];
                 }
             }
         }
@@ -473,21 +576,21 @@ __device__ __forceinline__ void gauss_out(const GaussArgs &a, const float (&dt)[
 }
 template <int TR>
 __device__ __forceinline__ void gauss_tile(const GaussArgs &a, int X0, int Y0) {
-    __shared__ float dt[down_th<TR>()][kDownTW];
-    __shared__ uint8_t it[down_th<TR>()][kDownTW];
-    const int ox = 2 * X0 - 2, oy = 2 * Y0 - 2;
-    if (a.do_depth) load_tile(a.dsrc, ox, oy, dt);
-    load_tile(a.isrc, ox, oy, it);
+    __shared__ GaussTile<TR> g;
+    const int ox = 2 * X0 - 4, oy = 2 * Y0 - 2;
+    gauss_stage<TR>(a, ox, oy, g);
+    __syncthreads();
+    gauss_rows<TR>(g);
     __syncthreads();
 #pragma unroll 1
-    for (int r = 0; r < TR / BY; ++r) gauss_out<TR>(a, dt, it, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
+    for (int r = 0; r < TR / BY; ++r) gauss_out<TR>(a, g, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
 }
 __global__ void k_gauss_down(GaussArgs a) {
     gauss_tile<kTileRowsSingle>(a, blockIdx.x * BX, blockIdx.y * kTileRowsSingle);
 }
 __global__ void k_gauss_down_b(const GaussArgs *A) {
     __shared__ GaussArgs sa;
-    gauss_tile<kTileRowsBatch>(stage_args(sa, A[blockIdx.z]), blockIdx.x * BX, blockIdx.y * kTileRowsBatch);
+    gauss_tile<kGaussRowsBatch>(stage_args(sa, A[blockIdx.z]), blockIdx.x * BX, blockIdx.y * kGaussRowsBatch);
 }
 
 __constant__ float c_sobel_x[9] = {0.52201f, 0.00000f, -0.52201f, 0.79451f, -0.00000f,
@@ -501,53 +604,91 @@ __constant__ float c_sobel_y[9] = {0.52201f, 0.79451f, 0.52201f, 0.00000f, 0.000
 // src/odom/reduce.cu:782-810: j0 < cols-5, i < rows-1, no zero intensity in
 // the [i-2, i+2) x [j0-2, j0+2) window, |grad|^2 >= minScale, depth not NaN)
 // into a byte mask, so the per-iteration pass reads one byte per pixel.
-// Non-zero test of the 4x4 intensity window [y-2, y+2) x [x-2, x+2) for the
-// 32 pixels of a warp (one tile row, lane = x - X0): tile row y - 2 - oy + u
-// holds window row u, tile columns lane .. lane + 3 its four pixels.  Each
-// tile row's non-zero bits over the 36 tile columns come from two ballots,
-// so a lane tests its window with shifts instead of 16 loads.  Tile entries
-// outside the image read 0 here; the caller uses the result for pixels
-// whose window lies inside the image only.  Executed by all 32 lanes.
+//
+// The block's source intensities are staged as floats (the values the
+// reference's taps convert them to), and each staged row's non-zero bits
+// over its 36 columns as one 64-bit mask (two ballots per row), so that a
+// pixel tests its 4x4 window with four broadcast loads and shifts.  Tile
+// entries outside the image read 0; the masks are used for pixels whose
+// window lies inside the image only.
+//
+// Interior Sobel sums: the reference accumulates all nine taps in order,
+// three of them with weight +-0 in each sum.  Those are no-ops: the taps are
+// intensities >= 0, so a zero-weight term is +-0, and the running sum is
+// never -0 (it starts at +0 and a round-to-nearest sum is -0 only when both
+// terms are), so adding +-0 returns it unchanged.  The six others are added
+// in the reference's order.
+// The staged tile starts 4 columns left of the block's first pixel (X0 - 4,
+// a multiple of 4) and is BX + 8 wide, filled by aligned 4-pixel loads.
+constexpr int kDerTW4 = BX + 8;
 template <int TR>
-__device__ __forceinline__ bool window_nonzero(const uint8_t (&t)[der_th<TR>()][kDerTW], int row0, int lane) {
-    bool ok = true;
+struct DerivTile {
+    __align__(16) float f[der_th<TR>()][kDerTW4];
+    unsigned long long nz[der_th<TR>()];
+};
+template <int TR>
+__device__ __forceinline__ void deriv_stage(const Img<const uint8_t> &src, int ox, int oy, DerivTile<TR> &t) {
+    constexpr int Q = kDerTW4 / 4, N = der_th<TR>() * Q, NT = BX * BY, IT = (N + NT - 1) / NT;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    const bool aligned = !(((uintptr_t)src.data | src.pitch) & 3);
+    unsigned v[IT];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const uint8_t *r = t[row0 + u];
-        const unsigned lo = __ballot_sync(0xffffffffu, r[lane] > 0);
-        const unsigned hi = __ballot_sync(0xffffffffu, lane < kDerTW - 32 && r[32 + (lane & 3)] > 0);
-        const unsigned long long m = ((unsigned long long)hi << 32) | lo;
-        ok = ok && ((m >> lane) & 0xFull) == 0xFull;
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
+        const int ty = i / Q, gx = ox + 4 * (i - ty * Q), gy = oy + ty;
+        v[k] = 0;
+        if (i < N && gy >= 0 && gy < src.rows) {
+            if (aligned && gx >= 0 && gx + 3 < src.cols) {
+                v[k] = *reinterpret_cast<const unsigned *>(&at(src, gx, gy));
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (gx + e >= 0 && gx + e < src.cols) v[k] |= (unsigned)at(src, gx + e, gy) << (8 * e);
+            }
+        }
     }
-    return ok;
+#pragma unroll
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
+        if (i < N) {
+            const int ty = i / Q, tx = 4 * (i - ty * Q);
+            *reinterpret_cast<float4 *>(&t.f[ty][tx]) =
+                make_float4((float)(v[k] & 0xffu), (float)((v[k] >> 8) & 0xffu), (float)((v[k] >> 16) & 0xffu),
+                            (float)(v[k] >> 24));
+        }
+    }
 }
 
 template <int TR>
-__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_t (&t)[der_th<TR>()][kDerTW], int ox,
-                                         int oy, int x, int y) {
+__device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const DerivTile<TR> &t, int ox, int oy, int x,
+                                         int y) {
     const Img<const uint8_t> src = a.src[l];
-    // the window test of the interior pixels, warp-wide (before any lane returns)
-    const bool win_ok = window_nonzero<TR>(t, y - 2 - oy, x - ox - 2);
     if (x >= src.cols || y >= src.rows) return;
+    // the depth the candidate test reads, loaded before the arithmetic
+    const float depth = at(a.depth[l], x, y);
     float dxVal = 0, dyVal = 0;
     if (x >= 1 && x <= src.cols - 2 && y >= 1 && y <= src.rows - 2) {
-        // interior: the same loop fully unrolled (kernelIndex = 8 - k)
-#pragma unroll
-        for (int jj = 0; jj < 3; ++jj) {
-            const uint8_t *r = t[y - 1 + jj - oy] - ox + x - 1;
-#pragma unroll
-            for (int ii = 0; ii < 3; ++ii) {
-                dxVal += (float)r[ii] * c_sobel_x[8 - (jj * 3 + ii)];
-                dyVal += (float)r[ii] * c_sobel_y[8 - (jj * 3 + ii)];
-            }
-        }
+        const float *r0 = &t.f[y - 1 - oy][x - 1 - ox], *r1 = r0 + kDerTW4, *r2 = r1 + kDerTW4;
+        // weights c_sobel_x[8 - k], c_sobel_y[8 - k] of tap k = 3 row + column
+        dxVal += r0[0] * -0.52201f;
+        dyVal += r0[0] * -0.52201f;
+        dyVal += r0[1] * -0.79451f;
+        dxVal += r0[2] * 0.52201f;
+        dyVal += r0[2] * -0.52201f;
+        dxVal += r1[0] * -0.79451f;
+        dxVal += r1[2] * 0.79451f;
+        dxVal += r2[0] * -0.52201f;
+        dyVal += r2[0] * 0.52201f;
+        dyVal += r2[1] * 0.79451f;
+        dxVal += r2[2] * 0.52201f;
+        dyVal += r2[2] * 0.52201f;
     } else {
         int kernelIndex = 8;
         for (int j = max(y - 1, 0); j <= min(y + 1, src.rows - 1); j++) {
-            const uint8_t *r = t[j - oy] - ox;
+            const float *r = t.f[j - oy] - ox;
             for (int i = max(x - 1, 0); i <= min(x + 1, src.cols - 1); i++) {
-                dxVal += (float)r[i] * c_sobel_x[kernelIndex];
-                dyVal += (float)r[i] * c_sobel_y[kernelIndex];
+                dxVal += r[i] * c_sobel_x[kernelIndex];
+                dyVal += r[i] * c_sobel_y[kernelIndex];
                 --kernelIndex;
             }
         }
@@ -560,27 +701,36 @@ __device__ __forceinline__ void deriv_px(const DerivArgs &a, int l, const uint8_
     if (j0 < cols - 5 && i < rows - 1) {
         bool valid = true;
         if (i >= 2 && j0 >= 2) {  // interior (i + 2 <= rows, j0 + 2 <= cols hold here)
-            valid = win_ok;
+            const int r = y - 2 - oy;
+            const unsigned long long m = t.nz[r] & t.nz[r + 1] & t.nz[r + 2] & t.nz[r + 3];
+            valid = ((m >> (x - 2 - ox)) & 0xFull) == 0xFull;
         } else {
             for (int u = max(i - 2, 0); u < min(i + 2, rows); u++) {
-                const uint8_t *r = t[u - oy] - ox;
+                const float *r = t.f[u - oy] - ox;
                 for (int v = max(j0 - 2, 0); v < min(j0 + 2, cols); v++) valid = valid && (r[v] > 0);
             }
         }
         if (valid) {
             float mTwo = (sx * sx) + (sy * sy);
-            c = mTwo >= a.minScale[l] && !isnan(at(a.depth[l], x, y));
+            c = mTwo >= a.minScale[l] && !isnan(depth);
         }
     }
     at(a.cand[l], x, y) = c ? 1 : 0;
 }
 template <int TR>
 __device__ __forceinline__ void deriv_tile(const DerivArgs &a, const LevelTiles &lt) {
-    __shared__ uint8_t t[der_th<TR>()][kDerTW];
+    __shared__ DerivTile<TR> t;
     int l, X0, Y0;
     tile_origin(lt, blockIdx.x, l, X0, Y0);
-    const int ox = X0 - 2, oy = Y0 - 2;
-    load_tile(a.src[l], ox, oy, t);
+    const int ox = X0 - 4, oy = Y0 - 2;
+    deriv_stage<TR>(a.src[l], ox, oy, t);
+    __syncthreads();
+    const int lane = threadIdx.x;
+    for (int r = threadIdx.y; r < der_th<TR>(); r += BY) {
+        const unsigned lo = __ballot_sync(0xffffffffu, t.f[r][lane] > 0);
+        const unsigned hi = __ballot_sync(0xffffffffu, lane < kDerTW4 - 32 && t.f[r][32 + (lane & 7)] > 0);
+        if (lane == 0) t.nz[r] = ((unsigned long long)hi << 32) | lo;
+    }
     __syncthreads();
 #pragma unroll 1
     for (int r = 0; r < TR / BY; ++r) deriv_px<TR>(a, l, t, ox, oy, X0 + threadIdx.x, Y0 + threadIdx.y + BY * r);
@@ -692,7 +842,7 @@ cudaError_t launch_rgbd_level0_batch(const RgbdArgs *args, int npairs, int max_c
     return cudaGetLastError();
 }
 cudaError_t launch_gauss_down_batch(const GaussArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
-    k_gauss_down_b<<<grid_tall(max_cols, max_rows, npairs, kTileRowsBatch), dim3(BX, BY), 0, s>>>(args);
+    k_gauss_down_b<<<grid_tall(max_cols, max_rows, npairs, kGaussRowsBatch), dim3(BX, BY), 0, s>>>(args);
     return cudaGetLastError();
 }
 cudaError_t launch_derivatives_batch(const DerivArgs *args, int npairs, int max_cols, int max_rows, cudaStream_t s) {
