@@ -75,6 +75,9 @@ def parse():
                          "precision: 1000 corridor pairs, FP32 vs compensated FP32 vs the FP64 oracle")
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
+    ap.add_argument("--corridor", default="tapered", choices=["tapered", "clutter"],
+                    help="precision study: clutter-free corridors with tapered walls (cond(JtJ) mostly 1e6-1e9) "
+                         "or straight corridors with 24 clutter spheres")
     ap.add_argument("--no-autotune", action="store_true", help="batch study: keep the default launch shape")
     ap.add_argument("--launch", default=None, help="batch study: fixed launch shape THREADSxPIXELS (e.g. 128x8)")
     ap.add_argument("--sizes", default="mixed", choices=["mixed", "640x480"],
@@ -1014,7 +1017,22 @@ PRECISION_FIELDS = ["pair", "cond", "inliers", "point", "relA_fp32", "relA_comp"
                     "count_diff_comp"]
 
 
-def precision_pair(i, seed, g32, gcomp, k64, cam, dist, angle):
+def precision_corridor(i, seed, cam, kind):
+    """Pair i of the precision study.  'tapered': no clutter, side walls
+    tapered by |taper| log-uniform in [2e-4, 4e-3] (random sign), which puts
+    cond(JtJ) of the level-0 ICP normal equations mostly in 1e6-1e9;
+    'clutter': straight walls and 24 clutter spheres (cond mostly 1e3-1e5,
+    or singular when no sphere is in view)."""
+    from slam_gb300 import synth
+    s = seed * 100000 + i
+    if kind == "clutter":
+        return synth.make_corridor_pair(s, cam=cam)
+    rng = np.random.default_rng(s ^ 0x7a9e)
+    taper = float(np.exp(rng.uniform(np.log(2e-4), np.log(4e-3)))) * (1.0 if rng.uniform() < 0.5 else -1.0)
+    return synth.make_corridor_pair(s, cam=cam, nclutter=0, taper=taper)
+
+
+def precision_pair(i, seed, g32, gcomp, k64, cam, dist, angle, kind="tapered"):
     """One corridor pair of the precision study: the ICP normal equations at
     level 0 (at the start pose and at the FP64 oracle's converged pose) as the
     tracker's FP32 and compensated-FP32 reductions deliver them, against the
@@ -1024,7 +1042,7 @@ def precision_pair(i, seed, g32, gcomp, k64, cam, dist, angle):
     import torch
     from slam_gb300 import synth
     from oracle import oracle
-    p = synth.make_corridor_pair(seed * 100000 + i, cam=cam)
+    p = precision_corridor(i, seed, cam, kind)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     devd = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int16)).cuda().view(torch.uint16)
     T1 = p["T1"]
@@ -1097,7 +1115,7 @@ def run_precision_study(args):
     t0 = time.time()
     rows, poses = [], []
     for i in range(args.pairs):
-        r, pr = precision_pair(i, args.seed, g32, gcomp, k64, cam, dist, angle)
+        r, pr = precision_pair(i, args.seed, g32, gcomp, k64, cam, dist, angle, args.corridor)
         rows += r
         poses.append(pr)
     elapsed = time.time() - t0
@@ -1128,17 +1146,37 @@ def run_precision_study(args):
         tr = np.array([p[name][1] for p in poses])
         pose[name] = {"rot_rad": pct(rot), "trans_m": pct(tr),
                       "frac_within_1e-5": float(np.mean((rot <= 1e-5) & (tr <= 1e-5)))}
+    # by the condition number of the FP64 JtJ at the start pose
+    bins = {}
+    start = {r["pair"]: r for r in rows if r["point"] == "start"}
+    for lo, hi, name in ((0, 1e4, "<1e4"), (1e4, 1e6, "1e4-1e6"), (1e6, 1e9, "1e6-1e9"), (1e9, np.inf, ">1e9")):
+        idx = [k for k, r in start.items() if lo <= r["cond"] < hi]
+        if not idx:
+            bins[name] = {"pairs": 0}
+            continue
+        b = {"pairs": len(idx)}
+        for name_ in ("fp32", "comp"):
+            med = lambda key: float(np.median([start[k][key + "_" + name_] for k in idx]))
+            rot = np.array([poses[k][name_][0] for k in idx])
+            tr = np.array([poses[k][name_][1] for k in idx])
+            b[name_] = {"relA_p50": med("relA"), "relb_p50": med("relb"), "inc_rot_p50": med("inc_rot"),
+                        "inc_trans_p50": med("inc_trans"), "pose_rot_p50": float(np.median(rot)),
+                        "pose_trans_p50": float(np.median(tr)),
+                        "frac_within_1e-5": float(np.mean((rot <= 1e-5) & (tr <= 1e-5)))}
+        bins[name] = b
     pose["fp64_oracle_vs_ground_truth"] = {"rot_rad": pct([p["fp64_vs_gt"][0] for p in poses]),
                                            "trans_m": pct([p["fp64_vs_gt"][1] for p in poses])}
     pose["fp32_vs_comp"] = {"rot_rad": pct([p["fp32_vs_comp"][0] for p in poses]),
                             "trans_m": pct([p["fp32_vs_comp"][1] for p in poses])}
+    corridor = ("no clutter, side walls tapered by 2e-4..4e-3 (log-uniform)" if args.corridor == "tapered"
+                else "24 clutter spheres, straight walls")
     out = {"study": "precision", "pairs": args.pairs, "data": "synthetic",
-           "config": {"workload": "low-texture corridor 2 m x 20 m, camera 1.5 m above the floor pitched down "
-                                  "25-40 deg, <= 3 deg / 5 cm relative motion, 640x480, 3 levels 10/5/4, "
-                                  "ICP+RGB (icpWeight 10), SO3 on",
+           "config": {"workload": "low-texture corridor 2 m x 20 m (" + corridor + "), camera 1.5 m above the "
+                                  "floor pitched down 25-40 deg, <= 3 deg / 5 cm relative motion, 640x480, 3 levels "
+                                  "10/5/4, ICP+RGB (icpWeight 10), SO3 on",
                       "jtj": "level-0 ICP sums at the start pose and at the FP64 oracle's converged pose; "
                              "FP64 reference = oracle on the same FP32 maps"},
-           "jtj_increment": summary, "pose_vs_fp64_oracle": pose, "elapsed_s": elapsed}
+           "jtj_increment": summary, "pose_vs_fp64_oracle": pose, "by_start_cond": bins, "elapsed_s": elapsed}
     print(json.dumps(out), flush=True)
 
 

@@ -46,7 +46,6 @@ struct PairBufs {
     Img<int16_t> dx[kLevels], dy[kLevels];
     Img<Corr> corr[kLevels];
     Img<uint8_t> cand[kLevels];
-    Img<float> vz, vzn;  // raw vertex z of the model / live maps (level 0)
     ReduceWs ws;
 };
 
@@ -234,8 +233,6 @@ int ensure_layout(odo_batch_t *b, const odo_pair *pairs, int n) {
             p.cand[l] = carve_img<uint8_t>(base, off, w, h);
             p.depn[l] = carve_img<float>(base, off, w, h);
         }
-        p.vz = carve_img<float>(base, off, p.w, p.h);
-        p.vzn = carve_img<float>(base, off, p.w, p.h);
         off = round_up(off, 256);
         p.ws.icp_part = (float *)(base + off);
         off += round_up(sizeof(float) * 32 * maxb, 256);
@@ -284,8 +281,8 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
         m.t[0] = q.pose[3];
         m.t[1] = q.pose[7];
         m.t[2] = q.pose[11];
-        m.vz = p.vz.data;
-        m.vz_pitch = p.vz.pitch;
+        m.vz = p.dep[0].data;  // the model's level-0 photometric depth, written by the import
+        m.vz_pitch = p.dep[0].pitch;
         std::memcpy(at(b->o_model) + i * sizeof(ModelArgs), &m, sizeof(m));
         // live maps (initICP(verts, norms)): planar pyramid, no transform,
         // raw vertex z for the live photometric depth
@@ -301,8 +298,8 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
                 lm.nmap[l] = p.nc[l];
             }
             lm.do_transform = 0;
-            lm.vz = p.vzn.data;
-            lm.vz_pitch = p.vzn.pitch;
+            lm.vz = p.depn[0].data;
+            lm.vz_pitch = p.depn[0].pitch;
             std::memcpy(at(b->o_live) + i * sizeof(ModelArgs), &lm, sizeof(lm));
         }
         // photometric depth of the live frame: the model's (depth input, the
@@ -314,11 +311,11 @@ void build_args(odo_batch_t *b, const odo_pair *pairs, int n, int rgbOnly, float
         const size_t sp[3] = {q.model_rgba_pitch, q.rgba_pitch, q.prev_rgba ? q.prev_rgba_pitch : q.rgba_pitch};
         Img<uint8_t> *imgs[3] = {p.last, p.next, p.lastnext};
         for (int r = 0; r < 3; ++r) {
-            // depth rows: the model's (role 0) and, for live maps, the live one (role 1)
+            // depth rows: the model's (role 0) and, for live maps, the live one
+            // (role 1); their level 0 is written by the map import
             const int with_depth = r == 0 || (r == 1 && live_maps);
             Img<float> *dp = r == 1 ? depn : p.dep;
-            const Img<float> &vzr = r == 1 ? p.vzn : p.vz;
-            RgbdArgs a{vzr.data, vzr.pitch, src[r], sp[r], dp[0], imgs[r][0], with_depth};
+            RgbdArgs a{nullptr, 0, src[r], sp[r], dp[0], imgs[r][0], 0};
             std::memcpy(at(b->o_rgbd[r]) + i * sizeof(RgbdArgs), &a, sizeof(a));
             for (int l = 0; l < 2; ++l) {
                 Img<const float> ds{dp[l].data, dp[l].pitch, dp[l].cols, dp[l].rows};
@@ -795,8 +792,19 @@ int odo_batch_track_warm(odo_batch_t *b, odo_cnn_t *net, const odo_pair *pairs, 
         reuse = reuse && pairs[i].levels <= wp->levels;
     }
     std::vector<odo_pair_result> sres(idx.size());
+    // The launch shape is tuned for whole batches; for a small subset it
+    // leaves the level-0 launch below one wave of long-running blocks.  The
+    // subset runs with fewer pixels per thread, halved until its level-0
+    // launch has at least 8 waves of blocks (3 resident per SM); the shape
+    // is restored after the call, so the cached graphs stay valid.
+    const int saved_ppt = b->ppt;
+    long long px = 0;
+    for (const odo_pair &q : sub) px += (long long)q.width * q.height;
+    const long long want_blocks = 8ll * 3 * (b->sm_count > 0 ? b->sm_count : 1);
+    while (b->ppt > 2 && px / ((long long)b->threads * b->ppt) < want_blocks) b->ppt >>= 1;
     rc = track_impl(b, sub.data(), (int)sub.size(), nullptr, wp->rgbOnly, wp->icpWeight, wp->fastOdom, 1, sres.data(),
                     false, reuse ? sub_slot.data() : nullptr);
+    b->ppt = saved_ppt;
     if (rc != ODO_OK) return rc;
     for (size_t k = 0; k < idx.size(); ++k) results[idx[k]] = sres[k];
     return ODO_OK;

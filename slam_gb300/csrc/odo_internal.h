@@ -132,6 +132,8 @@ struct ModelArgs {
     Map3 vmap[kLevels], nmap[kLevels];
     int do_transform;
     float R[9], t[3];
+    // level-0 photometric depth of these maps: the vertex z cut at 6 m
+    // (verticesToDepth), written beside the import
     float *vz;
     size_t vz_pitch;
 };

@@ -229,6 +229,13 @@ __global__ void k_vmap_nmap_b(const VNArgs *A, LevelTiles t) {
     vnmap_tile(stage_args(sa, A[blockIdx.z]), t);
 }
 
+// verticesToDepthKernel (src/odom/utils.cu:526-537): the photometric depth
+// of a vertex, cut at maxDepthRGB = 6.0 (src/odom/RGBDOdometryef.cpp:37).
+__device__ __forceinline__ float model_depth(float z) {
+    const float cutOff = 6.0f;
+    return z > cutOff || z <= 0 ? qnan_f() : z;
+}
+
 // copyMapsKernel (src/odom/utils.cu:270-310): a pixel is valid iff the
 // vertex z != 0.
 __device__ __forceinline__ void copy_px(const ModelArgs &a, int x, int y, float3 &v, float3 &n) {
@@ -307,7 +314,7 @@ __device__ __forceinline__ void model_tile(const ModelArgs &a, int tile) {
         v0[k] = n0[k] = make_float3(q, q, q);
         if (x < a.cols0 && y < a.rows0 && a.vmap[0].cols > 0) {
             copy_px(a, x, y, v0[k], n0[k]);
-            rowp(a.vz, a.vz_pitch, y)[x] = rowp(a.v4, a.pitch4, y)[4 * x + 2];
+            rowp(a.vz, a.vz_pitch, y)[x] = model_depth(rowp(a.v4, a.pitch4, y)[4 * x + 2]);
             store_model_px(a, a.vmap[0], a.nmap[0], x, y, v0[k], n0[k]);
         }
     }
@@ -332,16 +339,13 @@ __global__ void __launch_bounds__(256) k_model_maps_b(const ModelArgs *A) {
     model_tile(stage_args(sa, A[blockIdx.z]), blockIdx.x);
 }
 
-// verticesToDepthKernel (src/odom/utils.cu:526-537, cut at maxDepthRGB =
-// 6.0, src/odom/RGBDOdometryef.cpp:37) and bgr2IntensityKernel
-// (src/odom/utils.cu:550-563; RGBA input, so R is weighted 0.114).
+// The level-0 photometric images: the depth that the map import wrote
+// (verticesToDepthKernel's cut vertex z, see model_depth), copied, and
+// bgr2IntensityKernel (src/odom/utils.cu:550-563; RGBA input, so R is
+// weighted 0.114).
 __device__ __forceinline__ void rgbd_px(const RgbdArgs &a, int x, int y) {
     if (x >= a.img0.cols || y >= a.img0.rows) return;
-    if (a.do_depth) {
-        const float cutOff = 6.0f;
-        float z = rowp(a.vz, a.vz_pitch, y)[x];
-        at(a.depth0, x, y) = z > cutOff || z <= 0 ? qnan_f() : z;
-    }
+    if (a.do_depth) at(a.depth0, x, y) = rowp(a.vz, a.vz_pitch, y)[x];
     uchar4 src = *reinterpret_cast<const uchar4 *>(rowp(a.rgba, a.rgba_pitch, y) + 4 * x);
     int value = (float)src.x * 0.114f + (float)src.y * 0.299f + (float)src.z * 0.587f;
     at(a.img0, x, y) = value;
@@ -369,15 +373,9 @@ __device__ __forceinline__ void rgbd_px4(const RgbdArgs &a, int x0, int y) {
         packed |= ((unsigned)value & 0xffu) << (8 * k);
     }
     *reinterpret_cast<unsigned *>(&at(a.img0, x0, y)) = packed;
-    if (a.do_depth) {
-        const float cutOff = 6.0f;
-        const float4 z4 = *reinterpret_cast<const float4 *>(rowp(a.vz, a.vz_pitch, y) + x0);
-        const float zs[4] = {z4.x, z4.y, z4.z, z4.w};
-        float d[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) d[k] = zs[k] > cutOff || zs[k] <= 0 ? qnan_f() : zs[k];
-        *reinterpret_cast<float4 *>(&at(a.depth0, x0, y)) = make_float4(d[0], d[1], d[2], d[3]);
-    }
+    if (a.do_depth)
+        *reinterpret_cast<float4 *>(&at(a.depth0, x0, y)) =
+            *reinterpret_cast<const float4 *>(rowp(a.vz, a.vz_pitch, y) + x0);
 }
 __global__ void k_rgbd_level0(RgbdArgs a) {
     rgbd_px4(a, 4 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y * blockDim.y + threadIdx.y);

@@ -134,7 +134,21 @@ int synth_render(const synth_scene *s, const float pose_wc[16], int w, int h, fl
             // exit distance of the box interior
             double tbest = 1e30;
             int hit = -1;  // 0..5 walls, 6+k sphere k
+            const double taper = s->wall_taper;
             for (int k = 0; k < 3; ++k) {
+                if (k == 0 && taper != 0) {
+                    // tapered side walls x = bmax[0] + taper z, x = bmin[0] - taper z
+                    const double dr = d[0] - taper * d[2], dl = d[0] + taper * d[2];
+                    if (dr > 1e-12) {
+                        const double tk = (s->bmax[0] + taper * t[2] - t[0]) / dr;
+                        if (tk > 0 && tk < tbest) { tbest = tk; hit = 1; }
+                    }
+                    if (dl < -1e-12) {
+                        const double tk = (s->bmin[0] - taper * t[2] - t[0]) / dl;
+                        if (tk > 0 && tk < tbest) { tbest = tk; hit = 0; }
+                    }
+                    continue;
+                }
                 if (std::fabs(d[k]) < 1e-12) continue;
                 double tk = ((d[k] > 0 ? s->bmax[k] : s->bmin[k]) - t[k]) / d[k];
                 if (tk > 0 && tk < tbest) { tbest = tk; hit = 2 * k + (d[k] > 0 ? 1 : 0); }
@@ -164,6 +178,11 @@ int synth_render(const synth_scene *s, const float pose_wc[16], int w, int h, fl
                 int ax = hit / 2;
                 nw[0] = nw[1] = nw[2] = 0;
                 nw[ax] = (hit & 1) ? -1.0 : 1.0;
+                if (hit < 2 && taper != 0) {  // (-+1, 0, taper), unit length, facing the interior
+                    const double inv = 1.0 / std::sqrt(1.0 + taper * taper);
+                    nw[0] *= inv;
+                    nw[2] = taper * inv;
+                }
                 base = s->wall_col[hit];
             } else {
                 int k = hit - 6;

@@ -21,6 +21,9 @@ typedef struct {
     float tex_freq;   // texture cycles per metre
     float tex_amp;    // 0..1 texture contrast
     uint64_t tex_seed;
+    // the two x faces (side walls) tapered along z: x = bmax[0] + wall_taper z
+    // and x = bmin[0] - wall_taper z (0: the box faces)
+    float wall_taper;
 } synth_scene;
 }
 

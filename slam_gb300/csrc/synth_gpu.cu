@@ -65,7 +65,27 @@ __global__ void k_render(const synth_scene *scenes, const int *perms, const View
     for (int i = 0; i < 3; ++i) d[i] = V.R[i * 3] * dc[0] + V.R[i * 3 + 1] * dc[1] + V.R[i * 3 + 2] * dc[2];
     float tbest = 1e30f;
     int hit = -1;
+    const float taper = s.wall_taper;
     for (int k = 0; k < 3; ++k) {
+        if (k == 0 && taper != 0.f) {
+            // tapered side walls x = bmax[0] + taper z, x = bmin[0] - taper z
+            const float dr = d[0] - taper * d[2], dl = d[0] + taper * d[2];
+            if (dr > 1e-12f) {
+                const float tk = (s.bmax[0] + taper * V.t[2] - V.t[0]) / dr;
+                if (tk > 0 && tk < tbest) {
+                    tbest = tk;
+                    hit = 1;
+                }
+            }
+            if (dl < -1e-12f) {
+                const float tk = (s.bmin[0] - taper * V.t[2] - V.t[0]) / dl;
+                if (tk > 0 && tk < tbest) {
+                    tbest = tk;
+                    hit = 0;
+                }
+            }
+            continue;
+        }
         if (fabsf(d[k]) < 1e-12f) continue;
         const float tk = ((d[k] > 0 ? s.bmax[k] : s.bmin[k]) - V.t[k]) / d[k];
         if (tk > 0 && tk < tbest) {
@@ -100,6 +120,11 @@ __global__ void k_render(const synth_scene *scenes, const int *perms, const View
         const int ax = hit / 2;
         nw[0] = nw[1] = nw[2] = 0;
         nw[ax] = (hit & 1) ? -1.f : 1.f;
+        if (hit < 2 && taper != 0.f) {  // (-+1, 0, taper), unit length, facing the interior
+            const float inv = rsqrtf(1.f + taper * taper);
+            nw[0] *= inv;
+            nw[2] = taper * inv;
+        }
         base = s.wall_col[hit];
     } else {
         const int k = hit - 6;

@@ -21,7 +21,7 @@ class Scene(ctypes.Structure):
     _fields_ = [("bmin", ctypes.c_float * 3), ("bmax", ctypes.c_float * 3), ("nsph", ctypes.c_int),
                 ("sph", (ctypes.c_float * 4) * MAX_SPH), ("sph_col", (ctypes.c_float * 3) * MAX_SPH),
                 ("wall_col", (ctypes.c_float * 3) * 6), ("tex_freq", ctypes.c_float), ("tex_amp", ctypes.c_float),
-                ("tex_seed", ctypes.c_uint64)]
+                ("tex_seed", ctypes.c_uint64), ("wall_taper", ctypes.c_float)]
 
 
 def make_room(seed, nspheres=20):
@@ -146,12 +146,18 @@ def corridor_camera(rng):
     return pose(R, t)
 
 
-def make_corridor_pair(seed, cam=None, max_deg=3.0, max_m=0.05, nclutter=24, tex_amp=None):
+def make_corridor_pair(seed, cam=None, max_deg=3.0, max_m=0.05, nclutter=24, tex_amp=None, taper=0.0):
     """One frame pair of the precision study: a low-texture corridor seen
-    from corridor_camera, live frame at a relative motion <= max_deg/max_m."""
+    from corridor_camera, live frame at a relative motion <= max_deg/max_m.
+    taper != 0 tapers the side walls (x = +-(1 + taper z)): without clutter
+    the translation along the corridor is then observed only through the
+    walls' tilt, so the ICP normal equations' condition number grows as
+    1 / taper^2 (about 1e9.5 at 1e-4, 1e8 at 1e-3, 1e6 at 3e-3 for these
+    views); with taper 0 and no clutter that translation is unobservable."""
     cam = cam or Camera()
     rng = np.random.default_rng(seed + 0x5151)
     scene = make_corridor(seed, nclutter)
+    scene.wall_taper = float(taper)
     if tex_amp is not None:
         scene.tex_amp = tex_amp
     T1 = corridor_camera(rng)

@@ -11,11 +11,13 @@ def test_gpu_render_matches_cpu_render(gpu):
     from slam_gb300.warmstart import render_views
     cam = synth.Camera().scaled(320, 240)
     rng = np.random.default_rng(4)
-    scenes = [synth.make_room(11, 20), synth.make_corridor(3)]
-    poses = [synth.room_camera(rng), synth.corridor_camera(rng)]
-    seeds = [17, 29]
-    g = render_views(scenes, [0, 1], poses, seeds, cam, depth=True, rgba=True, model=True)
-    for i in range(2):
+    tapered = synth.make_corridor(5, 0)
+    tapered.wall_taper = 0.05
+    scenes = [synth.make_room(11, 20), synth.make_corridor(3), tapered]
+    poses = [synth.room_camera(rng), synth.corridor_camera(rng), synth.corridor_camera(rng)]
+    seeds = [17, 29, 31]
+    g = render_views(scenes, [0, 1, 2], poses, seeds, cam, depth=True, rgba=True, model=True)
+    for i in range(3):
         c = synth.render(scenes[i], poses[i], cam, noise_seed=seeds[i], depth=True, rgba=True, model=True)
         gv, gn = g["vert"][i].cpu().numpy(), g["norm"][i].cpu().numpy()
         hit = (c["vert"][..., 3] > 0) & (gv[..., 3] > 0)
