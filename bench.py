@@ -27,7 +27,8 @@ Arms:
                   reference itself cannot be built here), all host threads, on
                   pairs of the same distribution.
 Studies (--study): batch (mixed-resolution verification), precision
-(corridor pairs against the FP64 oracle), warm (the warm start in detail).
+(corridor pairs against the FP64 oracle), warm (the warm start in detail),
+phases (where the time of a warm-started batched step goes).
 Multi-GPU: replicas (a tracking call does not shard); each rank tracks its own
 copy of the workload; value = frames of all ranks / max time over ranks.
 """
@@ -70,9 +71,13 @@ def parse():
     ap.add_argument("--mode", default="graph", choices=["graph", "stream", "persistent"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--study", default=None, choices=[None, "batch", "precision", "warm"],
+    ap.add_argument("--study", default=None, choices=[None, "batch", "precision", "warm", "phases"],
                     help="batch: 512 mixed-resolution pairs per launch (batched verification); "
-                         "precision: 1000 corridor pairs, FP32 vs compensated FP32 vs the FP64 oracle")
+                         "precision: 1000 corridor pairs, FP32 vs compensated FP32 vs the FP64 oracle; "
+                         "phases: the time split of a warm-started batched step")
+    ap.add_argument("--nvtx-steps", action="store_true",
+                    help="phases study: only one warm-started and one plain step, inside the NVTX ranges "
+                         "warm_step / plain_step (for a profiler's launch list)")
     ap.add_argument("--pairs", type=int, default=None)
     ap.add_argument("--pairs-out", default=None, help="precision study: per-pair CSV path")
     ap.add_argument("--corridor", default="tapered", choices=["tapered", "clutter"],
@@ -1383,8 +1388,90 @@ def _nvtx(name, fn):
     return out
 
 
+def run_phases_study(args):
+    """The time split of a warm-started batched step of --batch-pairs 640x480
+    pairs (CUDA events around whole calls, no profiler): the step without
+    fall-backs; the same tracking from precomputed proposals (no network in
+    the step); the network alone; 1/1/1 iterations and one level-0
+    iteration (so the preprocessing and one iteration set separate); the
+    plain step; per-level iteration kernels.  The network is untrained
+    (its proposals only feed the 2/2/2 schedule, whose cost does not depend
+    on them)."""
+    import ctypes
+    import torch
+    from slam_gb300 import synth, warmstart as ws, _native
+    from slam_gb300.batch import BatchOdometry
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    nb = args.batch_pairs
+    b = BatchOdometry(nb, stream=stream.cuda_stream)
+    net = ws.WarmStartNet(max_batch=nb, stream=stream.cuda_stream)
+    pool = ws.make_room_pairs(args.seed * 31 + 1000, nb, synth.Camera(), 10.0, 0.10)
+    fps = pool.frame_pairs()
+    descs = b._descs(fps)
+    b.set_launch(256, 64)
+    L = _native.load()
+    nofb = dict(levels=3, iterations=(2, 2, 2), residual_limit=0.0, max_disagree_deg=0.0)
+    if args.nvtx_steps:
+        for _ in range(max(args.warmup, 3)):
+            b.track_warm(net, fps, descs=descs, **nofb)
+            b.track(fps, descs=descs)
+        _nvtx("warm_step", lambda: b.track_warm(net, fps, descs=descs, **nofb))
+        _nvtx("plain_step", lambda: b.track(fps, descs=descs))
+        print(json.dumps({"study": "phases", "nvtx_steps": ["warm_step", "plain_step"], "pairs": nb}), flush=True)
+        return
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, r
+
+    def descs_with(levels, its):
+        d = b._descs(fps)
+        for i in range(nb):
+            d[i].levels = levels
+            for l in range(3):
+                d[i].iterations[l] = its[l]
+        return d
+
+    prop = torch.empty((nb, 6), dtype=torch.float32, device="cuda")
+
+    def net_only():
+        assert L.odo_cnn_propose(net._h, descs, nb, ctypes.c_void_p(prop.data_ptr())) == 0
+        assert L.odo_cnn_wait(net._h) == 0
+
+    out = {"study": "phases", "pairs": nb, "steps": args.steps, "unit": "ms per step",
+           "config": {"workload": f"{nb} held-out 640x480 room pairs, warm schedule 3 levels 2/2/2 without SO3, "
+                                  "no fall-backs; untrained network"}}
+    out["warm_step_no_fallback"] = timed(lambda: b.track_warm(net, fps, descs=descs, **nofb))[0]
+    out["network_alone"] = timed(net_only)[0]
+    for key, levels, its in (("from_proposals_2_2_2", 3, (2, 2, 2)), ("from_proposals_1_1_1", 3, (1, 1, 1)),
+                             ("from_proposals_level0_once", 1, (1, 0, 0))):
+        d = descs_with(levels, its)
+        ms, res = timed(lambda: b.track_init(fps, prop, descs=d))
+        out[key] = {"ms": ms, "device_ms_first_kernel_to_last_solve": max(r.done_us for r in res) * 1e-3}
+    out["plain_step"] = timed(lambda: b.track(fps, descs=descs))[0]
+    out["iteration_kernels_ms"] = {"level%d" % l: dict(zip(("association", "photometric_and_solve", "whole"),
+                                                           b.time_iteration(l, 20))) for l in range(3)}
+    a, c, d = (out[k]["ms"] for k in ("from_proposals_2_2_2", "from_proposals_1_1_1", "from_proposals_level0_once"))
+    out["derived"] = {"network_on_the_critical_path": out["warm_step_no_fallback"] - a,
+                      "one_iteration_set_2_2_2_minus_1_1_1": a - c,
+                      "preprocessing_and_fixed_costs": c - (a - c)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.study == "phases":
+        run_phases_study(args)
+        return
     if args.study == "warm":
         run_warm_study(args)
         return
