@@ -395,8 +395,10 @@ int odo_debug_history(odo_t *h, double *out, int max_rows);
  * block partials live in one fixed device array of this library
  * (ODO_NOALLOC_SCRATCH_BYTES, held by every device that loads the library
  * until the process exits).
- *  - Images up to ODO_NOALLOC_MAX_PIXELS pixels (cols * rows); larger ones
- *    return ODO_ERR_SIZE without touching the GPU.
+ *  - Images up to ODO_NOALLOC_MAX_PIXELS pixels (cols * rows), and maps
+ *    whose 3 * rows * pitch_bytes stays below 4 GiB (the kernels address
+ *    them with 32-bit offsets); others return ODO_ERR_SIZE without touching
+ *    the GPU.
  *  - The first call on a device looks up the array's device address (once
  *    per device, with that device current); make that first call before any
  *    stream capture.

@@ -55,4 +55,23 @@ __device__ __forceinline__ float *map_row(const Map3 &m, int c, int y) {
     return rowp(m.data, m.pitch, c * m.rows + y);
 }
 
+// The same addresses with a 32-bit byte offset (one 32-bit multiply-add and
+// one 64-bit add instead of a 64-bit product), for the per-pixel loads and
+// stores of the iteration passes.  Valid where the row index is not
+// negative and every offset stays below 4 GiB: the library's own images and
+// maps (frames of at most 8192 x 8192: the largest, the 16-byte
+// correspondence records, spans 1 GiB) and caller maps whose 3 x rows x
+// pitch the allocation-free entry point checks.
+template <typename T>
+__device__ __forceinline__ T &at32(T *base, size_t pitch, int x, int y) {
+    return *(T *)((char *)base + ((unsigned)y * (unsigned)pitch + (unsigned)x * (unsigned)sizeof(T)));
+}
+template <typename T>
+__device__ __forceinline__ T &at32(const Img<T> &im, int x, int y) {
+    return at32(im.data, im.pitch, x, y);
+}
+__device__ __forceinline__ float &map_at32(const Map3 &m, int c, int x, int y) {
+    return at32(m.data, m.pitch, x, c * m.rows + y);
+}
+
 }  // namespace slamgb
