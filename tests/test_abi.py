@@ -48,6 +48,26 @@ def test_argument_validation_without_gpu(built):
     assert L.odo_status_string(5) == b"device-side wait timed out"
 
 
+def test_noalloc_extent_checks_without_gpu(built):
+    """The allocation-free entry point refuses oversized images and maps
+    whose 3 x rows x pitch reaches 4 GiB (its kernels use 32-bit byte
+    offsets) before any CUDA call: the map pointers here are never read."""
+    from slam_gb300 import _native
+    L = _native.load()
+    fake = ctypes.c_void_p(256)
+    f = lambda n, v=0.0: (ctypes.c_float * n)(*([v] * n))
+    out = lambda n: (ctypes.c_float * n)()
+
+    def call(pitch, cols, rows):
+        return L.odo_icp_step_noalloc(fake, fake, fake, fake, pitch, cols, rows, f(4, 1.0), 0.1, 0.34, f(9), f(3),
+                                      f(9), f(3), None, out(36), out(6), out(2))
+    ODO_ERR_ARG, ODO_ERR_SIZE = 1, 6
+    assert call(640 * 4 - 4, 640, 480) == ODO_ERR_ARG             # pitch below one row
+    assert call(2048 * 4, 2048, 1024) == ODO_ERR_SIZE              # more than ODO_NOALLOC_MAX_PIXELS
+    assert call(1 << 31, 640, 480) == ODO_ERR_SIZE                 # 3 x 480 x 2 GiB >= 4 GiB
+    assert call((1 << 32) // (3 * 480) + 4, 640, 480) == ODO_ERR_SIZE
+
+
 def test_default_thresholds_match_reference_expression():
     """ODO_DEFAULT_ANGLE_THRESH is sin(20.f * 3.14159254f / 180.f) rounded to
     float, as the reference evaluates its default (src/odom/RGBDOdometryef.h:36),
